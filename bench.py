@@ -1,0 +1,451 @@
+"""Benchmark of the BCSR SpMM hot path on GB300 (one JSON line on stdout).
+
+Workload (the mixed-precision configuration the headline metric is quoted on):
+  A 16384 x 16384 with 64x16 blocks, random block pattern at 2 % block density,
+  block values N(0,1) x 10^u (u ~ U[-3, 3] per block); B 16384 x 512 N(0,1);
+  C = A B in fp32. Synthetic, seeded.
+  One step = one SpMM over one problem. Six copies of the problem (inputs and
+  output, ~370 MB > 2.5 x L2) are used round-robin so no step reads another
+  step's data from L2.
+
+Arms:
+  (default) this library: every precision (fp16, bf16, e4m3 + per-block scales,
+            split fp16 hi+lo) is autotuned over the kernel configurations; the
+            headline `value` is the fastest precision whose documented error bar
+            (tests/test_gpu_precision.py) is <= 1e-2 relative to FP64; plain fp16
+            is reported beside it.
+  --impl reference: the reference's host multiply (cpu_matmul_ref,
+            nvbench_main.cu:78-91, restated in oracle/) on all host cores, over a
+            bounded row sample per step, in the same unit.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M = K = 16384
+N = 512
+BR = 64
+DENSITY = 0.02
+SEED = 20240
+WORKLOAD = ("A 16384x16384, 64x16 blocks, random 2% block density, values N(0,1)*10^U[-3,3] "
+            "per block; B 16384x512 N(0,1); C fp32")
+METRIC = "BCSR SpMM TFLOP/s (nonzero-block FLOPs), tuned mixed precision vs plain FP16"
+# Documented normwise error bars vs FP64 (tests/test_gpu_precision.py).
+ERROR_BAR = {"f16": 2e-3, "bf16": 1e-2, "f16_split": 2e-6, "e4m3": 8e-2}
+TARGET_ERR = 1e-2
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def make_structure():
+    import matrixmultiplicationcuda_gb300 as m
+    rp, ci = m.gen_structure(M, K, BR, m.PATTERN_RANDOM, DENSITY, 0, seed=SEED)
+    return rp, ci
+
+
+def work_units(rp, ci):
+    nnzb = len(ci)
+    flops = 2.0 * nnzb * BR * 16 * N
+    cols_touched = len(np.unique(ci))
+    return nnzb, flops, cols_touched
+
+
+# bytes per stored element of A and of B, and per-block scale bytes, by precision
+STORAGE = {"f16": (2, 2, 0), "bf16": (2, 2, 0), "e4m3": (1, 1, 4), "f16_split": (4, 4, 0)}
+
+
+def algorithmic_bytes(nnzb, cols_touched, prec="f16"):
+    """Compulsory bytes of one SpMM: A values (+ e4m3 block scales) + col_idx +
+    row_ptr + the B rows that are referenced + the fp32 C write."""
+    a_es, b_es, sc = STORAGE[prec]
+    return (nnzb * BR * 16 * a_es + nnzb * sc + 4 * nnzb + 4 * (M // BR + 1) +
+            cols_touched * 16 * N * b_es + M * N * 4)
+
+
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) in the background."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.samples = []
+        self.proc = None
+        self.marks = {}
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.time(), parts))
+
+    def mark(self, name):
+        self.marks[name] = time.time()
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        t0, t1 = self.marks.get("timed_start", 0), self.marks.get("timed_end", 1e30)
+        w0 = self.marks.get("load_start", 0)
+        timed = [s for t, s in self.samples if t0 <= t <= t1]
+        window = "timed"
+        if len(timed) < 3:   # a short timed region: add the sustained load just before it
+            timed = [s for t, s in self.samples if w0 <= t <= t1]
+            window = "warmup+timed"
+        if not timed:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [num(s[1]) for s in timed if num(s[1])]
+        mx = [num(s[2]) for s in timed if num(s[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in timed for i in range(4) if s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(timed), "window": window}
+
+
+# ------------------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample_rows(rp, ci, vals_f32, B_half_bits, rows, row0):
+    """Dense fp16 rows [row0, row0+rows) of A (what the reference host multiply reads)."""
+    K16 = K
+    A = np.zeros((rows, K16), np.float16)
+    br0, br1 = row0 // BR, (row0 + rows + BR - 1) // BR
+    blocks = vals_f32.reshape(-1, BR, 16)
+    for br in range(br0, br1):
+        for k in range(rp[br], rp[br + 1]):
+            r_lo = max(br * BR, row0)
+            r_hi = min((br + 1) * BR, row0 + rows)
+            A[r_lo - row0:r_hi - row0, ci[k] * 16:(ci[k] + 1) * 16] = blocks[k][r_lo - br * BR:r_hi - br * BR]
+    return A
+
+
+def useful_flops_rows(rp, row0, rows):
+    """Nonzero-block FLOPs of output rows [row0, row0+rows)."""
+    f = 0.0
+    for br in range(row0 // BR, (row0 + rows + BR - 1) // BR):
+        lo, hi = max(br * BR, row0), min((br + 1) * BR, row0 + rows)
+        f += 2.0 * (rp[br + 1] - rp[br]) * 16 * (hi - lo) * N
+    return f
+
+
+def cpu_reference_rate(rp, ci, vals, Bbits, rows, threads, min_seconds=0.0, row0=0):
+    """TFLOP/s (nonzero-block) of the restated reference host multiply on `rows` rows."""
+    from oracle import oracle
+    A = cpu_sample_rows(rp, ci, vals, Bbits, rows, row0)
+    done, t = 0.0, 0.0
+    while True:
+        t0 = time.perf_counter()
+        oracle.cpu_matmul_ref(A.view(np.uint16), Bbits, threads=threads)
+        t += time.perf_counter() - t0
+        done += useful_flops_rows(rp, row0, rows)
+        if t >= min_seconds:
+            break
+    return done / t / 1e12, t
+
+
+# ------------------------------------------------------------------------------------
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import matrixmultiplicationcuda_gb300 as m
+    rp, ci = make_structure()
+    nnzb = len(ci)
+    vals = m.gen_values(nnzb, BR, 16, m.DIST_SCALED_NORMAL, seed=SEED + 1).astype(np.float16).astype(np.float32)
+    B = m.gen_dense(K, N, m.DIST_NORMAL, seed=SEED + 2).astype(np.float16)
+    threads = os.cpu_count() or 1
+    rows = 64 * threads          # bounded sample per step, ~1 s on 16 cores
+    for i in range(args.warmup):
+        cpu_reference_rate(rp, ci, vals, B.view(np.uint16), min(rows, 256), threads, row0=(i * 977) % (M - rows))
+    t_total, f_total = 0.0, 0.0
+    for i in range(args.steps):
+        r0 = (i * 1931) % (M - rows)
+        r0 -= r0 % BR
+        A = cpu_sample_rows(rp, ci, vals, B.view(np.uint16), rows, r0)
+        from oracle import oracle
+        t0 = time.perf_counter()
+        oracle.cpu_matmul_ref(A.view(np.uint16), B.view(np.uint16), threads=threads)
+        t_total += time.perf_counter() - t0
+        f_total += useful_flops_rows(rp, r0, rows)
+    value = f_total / t_total / 1e12
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "sample": "%d output rows per step" % rows},
+            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                             "sample": "%d of %d output rows per step, reference host multiply "
+                                       "(dense i-k-j, fp32) split by rows over %d threads" % (rows, M, threads)},
+            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import matrixmultiplicationcuda_gb300 as m
+    from matrixmultiplicationcuda_gb300 import DType
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    hbm_peak, tensor_peak, peak_kind = peaks()
+
+    rp, ci = make_structure()
+    nnzb, flops, cols_touched = work_units(rp, ci)
+    vals = m.gen_values(nnzb, BR, 16, m.DIST_SCALED_NORMAL, seed=SEED + 1)
+    Bf = m.gen_dense(K, N, m.DIST_NORMAL, seed=SEED + 2)
+
+    # device copies of the problem (six, round-robin) per precision
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
+    per_copy = algorithmic_bytes(nnzb, cols_touched, "f16")
+    copies = max(2, math.ceil(2.5 * l2 / per_copy))
+    rp_d = torch.from_numpy(rp).to(dev)
+    ci_d = torch.from_numpy(ci).to(dev)
+    v32 = torch.from_numpy(vals).to(dev)
+    B32 = torch.from_numpy(Bf).to(dev)
+
+    precs = {"f16": DType.F16, "bf16": DType.BF16, "e4m3": DType.E4M3, "f16_split": DType.F16_SPLIT}
+    if args.precision != "auto":
+        precs = {args.precision: precs[args.precision], "f16": DType.F16}
+
+    def prepare(dt):
+        out = []
+        for c in range(copies):
+            qv, qlo, qs = m.quantize(v32, dt, block_elems=BR * 16)
+            Bq, Blo, Bs = m.quantize(B32.reshape(-1), dt)
+            A = m.BCSR(M, K, BR, 16, rp_d.clone(), ci_d.clone(), qv, dt, qlo, qs)
+            C = torch.empty((M, N), dtype=torch.float32, device=dev)
+            out.append((A, Bq.view(K, N), Blo.view(K, N) if Blo is not None else None,
+                        float(Bs[0]) if Bs is not None else 1.0, C))
+        return out
+
+    def launch(prob, cfg, stream=None):
+        A, Bq, Blo, bs, C = prob
+        m.spmm(A, Bq, N=N, C=C, cfg=cfg, B_lo=Blo, b_scale=bs, stream=stream)
+
+    stream = torch.cuda.current_stream()
+
+    def time_loop(probs, cfg, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            launch(probs[i % len(probs)], cfg)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    # autotune every precision over the instantiated kernel configurations
+    cands = [m.Config(kernel=k, n_tile=nt, stages=st) for k, nt, st in
+             [(2, 0, 0), (1, 128, 4), (1, 128, 8), (1, 64, 4), (1, 256, 4)]]
+    results = {}
+    prepared = {}
+    sampler = ClockSampler(local)
+    sampler.start()
+    sampler.mark("load_start")
+    for name, dt in precs.items():
+        probs = prepare(dt)
+        prepared[name] = probs
+        best = None
+        for cfg in cands:
+            try:
+                time_loop(probs, cfg, 3)
+                m.device_error_check()
+            except m.SpmmError:
+                continue
+            t = time_loop(probs, cfg, 30)
+            if best is None or t < best[0]:
+                best = (t, cfg)
+        results[name] = {"ms": best[0], "cfg": best[1], "tflops": flops / best[0] / 1e9,
+                         "err_bar": ERROR_BAR[name], "bytes": algorithmic_bytes(nnzb, cols_touched, name)}
+    ok = {k: v for k, v in results.items() if v["err_bar"] <= TARGET_ERR}
+    tuned = min(ok, key=lambda k: results[k]["ms"])
+    probs, cfg = prepared[tuned], results[tuned]["cfg"]
+
+    # warm-up, then exactly K timed steps on the tuned configuration
+    t_warm = time.time()
+    w = 0
+    while w < args.warmup or time.time() - t_warm < 1.0:
+        launch(probs[w % len(probs)], cfg)
+        w += 1
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.mark("timed_start")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        launch(probs[i % len(probs)], cfg)
+        ev[i][1].record(stream)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    sampler.mark("timed_end")
+    barrier(world)
+    m.device_error_check()
+    total_ms = g0.elapsed_time(g1)
+    kern_ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    total_ms = max_over_ranks(total_ms, world)
+    ms_step = total_ms / args.steps
+    value = world * flops / (ms_step * 1e-3) / 1e12
+
+    # end to end through the public API with host buffers (pinned), tuned precision
+    A0, Bq0, Blo0, bs0, C0 = probs[0]
+    hA = [t.cpu().pin_memory() for t in (A0.row_ptr, A0.col_idx, A0.vals) if t is not None]
+    hx = [t.cpu().pin_memory() for t in (A0.vals_lo, A0.scales) if t is not None]
+    hB = [t.cpu().pin_memory() for t in (Bq0, Blo0) if t is not None]
+    hC = torch.empty((M, N), dtype=torch.float32).pin_memory()
+    dA = [torch.empty_like(t, device=dev) for t in hA]
+    dx = [torch.empty_like(t, device=dev) for t in hx]
+    dB = [torch.empty_like(t, device=dev) for t in hB]
+    h2d = sum(t.numel() * t.element_size() for t in hA + hx + hB)
+    d2h = hC.numel() * 4
+    Ae = m.BCSR(M, K, BR, 16, dA[0], dA[1], dA[2], A0.dtype,
+                dx[0] if A0.vals_lo is not None else None,
+                dx[-1] if A0.scales is not None else None)
+
+    def e2e_step():
+        for d, h in zip(dA + dx + dB, hA + hx + hB):
+            d.copy_(h, non_blocking=True)
+        m.spmm(Ae, dB[0], N=N, C=C0, cfg=cfg, B_lo=dB[1] if len(dB) > 1 else None, b_scale=bs0)
+        hC.copy_(C0, non_blocking=True)
+    e2e_steps = max(3, min(args.steps, 50))
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    q1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(q0.elapsed_time(q1) / e2e_steps, world)
+    sampler.stop()
+    clocks = sampler.summary()
+
+    # CPU baseline (reference host multiply, restated), rank 0 only, bounded sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        vh = vals.astype(np.float16).astype(np.float32)
+        Bh = Bf.astype(np.float16).view(np.uint16)
+        rate, secs = cpu_reference_rate(rp, ci, vh, Bh, 192, 1, min_seconds=10.0)
+        cpu = {"value": rate, "unit": "TFLOP/s", "cores": 1, "kind": "port",
+               "sample": "192 of %d output rows, reference host multiply (dense i-k-j, fp32, "
+                         "one thread), repeated for %.1f s" % (M, secs)}
+
+    tr = results[tuned]
+    bytes_launch = tr["bytes"]
+    achieved = bytes_launch / (kern_ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(tuned)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": tuned, "data": "synthetic (seeded generators)",
+            "config": {"workload": WORKLOAD, "precision": tuned,
+                       "kernel_config": {"kernel": cfg.kernel, "n_tile": cfg.n_tile, "stages": cfg.stages},
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
+                       "nnzb": nnzb},
+            "plain_fp16": {"tflops": results["f16"]["tflops"], "ms": results["f16"]["ms"]},
+            "tuned_vs_plain_fp16": results["f16"]["ms"] / tr["ms"],
+            "precisions": {k: {"tflops": v["tflops"], "ms": v["ms"], "err_bar": v["err_bar"],
+                               "kernel": v["cfg"].kernel, "n_tile": v["cfg"].n_tile, "stages": v["cfg"].stages}
+                           for k, v in results.items()},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "algorithmic_bytes": bytes_launch, "peak_source": peak_kind,
+                         "tensor_frac": (flops / (kern_ms * 1e-3) / 1e12) / tensor_peak},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "f16", "bf16", "e4m3", "f16_split"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * bcsr_spmm.h -- C ABI of the GB300 (sm_103a) BCSR sparse x dense multiply.
+ *
+ *   C (M x N, fp32, row-major) = A (M x K, BCSR, bR x 16 blocks) * B (K x N, row-major)
+ *
+ * Every entry point takes plain pointers and sizes, returns an spmm_status and
+ * never aborts. Device pointers are CUDA device (or managed) addresses; a
+ * `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ * Launches are asynchronous on that stream unless the comment says otherwise.
+ *
+ * The BCSR layout is the reference's BCSRMatrix (formats/BCSRMatrix.cuh:9-26,
+ * built in formats/BCSRMatrix.cu:22-74): row_ptr ("hdr") has M/bR + 1 ints,
+ * col_idx ("idx") has nnzb ints in units of 16 columns of A (= 16 rows of B),
+ * and the values hold nnzb blocks of bR x 16 elements, each block row-major and
+ * contiguous, blocks in row-major block order.
+ */
+#ifndef BCSR_SPMM_H
+#define BCSR_SPMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum spmm_status {
+  SPMM_OK = 0,
+  SPMM_ERR_INVALID_ARG = 1,    /* null pointer, negative size, bad block shape   */
+  SPMM_ERR_UNSUPPORTED = 2,    /* a shape or dtype this build has no kernel for  */
+  SPMM_ERR_MISALIGNED = 3,     /* a pointer or leading dimension breaks TMA rules */
+  SPMM_ERR_CUDA = 4,           /* a CUDA runtime / driver call failed             */
+  SPMM_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up              */
+  SPMM_ERR_BAD_STRUCTURE = 6,  /* row_ptr / col_idx failed validation             */
+  SPMM_ERR_SCRATCH_TOO_SMALL = 7
+} spmm_status;
+
+/* Storage / arithmetic type of A and B. All accumulate in fp32 and write fp32 C. */
+typedef enum spmm_dtype {
+  SPMM_F16 = 0,        /* A, B fp16 (the reference's type)                               */
+  SPMM_BF16 = 1,       /* A, B bf16                                                      */
+  SPMM_E4M3 = 2,       /* A e4m3 + one fp32 scale per block, B e4m3 + one fp32 scale     */
+  SPMM_F16_SPLIT = 3   /* A = A_hi + A_lo, B = B_hi + B_lo (fp16 pairs), 3 products      */
+} spmm_dtype;
+
+/* Kernel configuration. Zero-initialised = let the library choose. */
+typedef struct spmm_config {
+  int kernel;    /* 0 = auto, 1 = mma.sync pipeline, 2 = tcgen05 pipeline (bR = 64)  */
+  int n_tile;    /* output columns per CTA tile: 64, 128 or 256 (0 = auto)           */
+  int stages;    /* pipeline depth 2..8 (0 = auto)                                   */
+  int ctas_per_sm; /* persistent grid = SMs x this (0 = auto)                          */
+} spmm_config;
+
+/* Describes A. All arrays are device pointers. */
+typedef struct spmm_bcsr_desc {
+  int M, K;              /* rows / columns of A: multiples of bR and 16              */
+  int bR, bC;            /* block shape: bR in {16, 32, 64}, bC == 16                */
+  const int* row_ptr;    /* M/bR + 1 entries                                         */
+  const int* col_idx;    /* nnzb entries (col_idx / vals may be NULL when nnzb == 0)  */
+  const void* vals;      /* nnzb * bR * 16 elements of dtype (A_hi for F16_SPLIT)     */
+  const void* vals_lo;   /* F16_SPLIT: A_lo, same layout; otherwise NULL             */
+  const float* scales;   /* E4M3: nnzb per-block fp32 scales; otherwise NULL         */
+  spmm_dtype dtype;
+} spmm_bcsr_desc;
+
+/* Describes B (K x N row-major, leading dimension ldb >= N, in elements). */
+typedef struct spmm_dense_desc {
+  const void* data;      /* K x ldb elements (B_hi for F16_SPLIT)                    */
+  const void* data_lo;   /* F16_SPLIT: B_lo; otherwise NULL                          */
+  float scale;           /* E4M3: the fp32 scale of B (B = scale * stored); else 1   */
+  int ldb;
+} spmm_dense_desc;
+
+/* ---- library ------------------------------------------------------------------ */
+int spmm_abi_version(void);
+/* Text of the last error on the calling host thread ("" if none). */
+const char* spmm_last_error(void);
+
+/* ---- general entry point -------------------------------------------------------
+ * C[M x N] (ldc >= N, in floats) = A * B. Every C element in the M x N window is
+ * written (rows whose block row is empty get zeros), so C need not be cleared.
+ * N must be a multiple of 8 and ldb a multiple of 8 (16-byte TMA strides);
+ * E4M3 needs multiples of 16. cfg may be NULL.
+ */
+spmm_status spmm_bcsr_mm(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N,
+                         float* C, int ldc, const spmm_config* cfg, void* stream);
+
+/* Checks row_ptr / col_idx on the device (monotone, row_ptr[0] == 0,
+ * row_ptr[M/bR] == nnzb, col_idx in [0, K/16), strictly ascending within a
+ * row); col_idx is read only after row_ptr passed. Synchronises the stream.
+ * The reference never validates (its kernels trust hdr/idx). */
+spmm_status spmm_bcsr_validate(const int* row_ptr, const int* col_idx, int M, int K, int bR,
+                               long long nnzb, void* stream);
+
+/* ---- reference-shaped launchers ------------------------------------------------
+ * Drop-ins for the launch sites of the reference's __global__ kernels
+ * (src/cuda_kernels.cuh:39-114): the same argument list (hdr, idx, data, B, C,
+ * M, N) with fp16 data and B, plus K (the row count of B, which the
+ * reference's kernels never read because they trust idx; every reference call
+ * site has it) and the stream of the launch configuration. The grid, block and
+ * shared-memory sizes are chosen here. */
+
+/* 16x16 blocks: src/cuda_kernels.cu:301-328 (launch nvbench_main.cu:339-346).   */
+spmm_status sparseMatrixMulTensor_launch(const int* hdr, const int* idx, const void* data,
+                                         const void* B, float* C, unsigned M, unsigned N,
+                                         unsigned K, void* stream);
+/* 32x16 blocks: src/cuda_kernels.cu:699-762 (launch nvbench_main.cu:648-655).   */
+spmm_status sparseMatrixMulTensor32x16_launch(const int* hdr, const int* idx, const void* data,
+                                              const void* B, float* C, unsigned M, unsigned N,
+                                              unsigned K, void* stream);
+/* 64x16 blocks: src/cuda_kernels.cu:618-695 (launch nvbench_main.cu:548-555).   */
+spmm_status sparseMatrixMulTensor64x16_launch(const int* hdr, const int* idx, const void* data,
+                                              const void* B, float* C, unsigned M, unsigned N,
+                                              unsigned K, void* stream);
+/* Variant kernels of the reference compute the same product with other warp
+ * splits; each maps onto the launcher of its block shape:
+ *   _v2 (:370-417), _v3 (:423-489), _v1_improved (:495-547)          -> 16x16
+ *   32x16_v2 (:1001-1050), 32x16_shared (:768-845),
+ *   32x16_shared_vectorized (:853-934), 32x16_v2_shared_vectorized (:1056-1166) -> 32x16
+ *   64x16_v2 (:939-996)                                               -> 64x16
+ *   Adaptive / Adaptive32x16 / Adaptive64x16 (:1171-1363): colBlocksPerRow is
+ *   accepted and ignored (the persistent schedule balances the columns). */
+spmm_status sparseMatrixMulTensorAdaptive_launch(const int* hdr, const int* idx, const void* data,
+                                                 const void* B, float* C, unsigned M, unsigned N,
+                                                 unsigned colBlocksPerRow, unsigned K, void* stream);
+spmm_status sparseMatrixMulTensorAdaptive32x16_launch(const int* hdr, const int* idx,
+                                                      const void* data, const void* B, float* C,
+                                                      unsigned M, unsigned N,
+                                                      unsigned colBlocksPerRow, unsigned K,
+                                                      void* stream);
+spmm_status sparseMatrixMulTensorAdaptive64x16_launch(const int* hdr, const int* idx,
+                                                      const void* data, const void* B, float* C,
+                                                      unsigned M, unsigned N,
+                                                      unsigned colBlocksPerRow, unsigned K,
+                                                      void* stream);
+
+/* ---- dense -> BCSR on the GPU (BCSRMatrix ctor, formats/BCSRMatrix.cu:22-74) ---
+ * Bit-exact to the reference: a block is kept when any of its fp16 elements
+ * compares != 0 as a float (so -0 is zero and NaN is not), blocks in row-major
+ * block order, explicit zeros inside kept blocks are stored.
+ * Step 1 writes row_ptr (M/bR + 1 ints, device) and returns nnzb in *nnzb_out
+ * (synchronises the stream). Step 2 fills col_idx (nnzb ints) and vals
+ * (nnzb * bR * bC halves). A is M x K fp16 row-major on the device, lda >= K.
+ * Block sizes follow the ctor's checks (:24-34): multiples of 16, >= 16; this
+ * library's kernels then need bC == 16. M and K are truncated to whole blocks
+ * like the ctor (:37-38). */
+spmm_status spmm_dense_to_bcsr_count(const void* A, int M, int K, int lda, int bR, int bC,
+                                     int* row_ptr, long long* nnzb_out, void* stream);
+spmm_status spmm_dense_to_bcsr_fill(const void* A, int M, int K, int lda, int bR, int bC,
+                                    const int* row_ptr, int* col_idx, void* vals, void* stream);
+
+/* ---- precision conversion (device, asynchronous) ------------------------------
+ * From fp32 block values (the exact values before storage rounding):
+ *   to fp16 / bf16 (round to nearest even),
+ *   to e4m3 with one scale per block (scale = max|block| / 448, 1 for all-zero blocks),
+ *   to an fp16 hi/lo pair (hi = fp16(x), lo = fp16(x - hi)).
+ * `count` elements, `block_elems` elements per scale block (E4M3 only). */
+spmm_status spmm_quantize(const float* src, size_t count, spmm_dtype dtype, int block_elems,
+                          void* dst, void* dst_lo, float* scales, void* stream);
+
+/* ---- batched: many independent SpMMs in one persistent launch -----------------
+ * problems[i] describes one product; all must share dtype (F16 or BF16).
+ * The launch walks one work queue of (problem, block row, column tile) items,
+ * heaviest first. `plan` is an opaque host handle built once per batch
+ * (it owns a device copy of the problem table and the ordered queue). */
+typedef struct spmm_problem {
+  spmm_bcsr_desc A;
+  spmm_dense_desc B;
+  int N;
+  float* C;
+  int ldc;
+} spmm_problem;
+typedef struct spmm_batch_plan spmm_batch_plan;
+spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count,
+                                   const spmm_config* cfg, spmm_batch_plan** plan_out);
+spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream);
+spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
+
+/* ---- diagnostics ---------------------------------------------------------------
+ * Runs one block of the pipeline's bounded mbarrier wait on a barrier that no
+ * one arrives on, with the given limit in nanoseconds; returns SPMM_ERR_TIMEOUT
+ * when the wait gave up and the kernel exited cleanly (synchronises). */
+spmm_status spmm_debug_wait_timeout(unsigned long long timeout_ns, void* stream);
+/* Synchronises the stream, then reads and clears the device error word that the
+ * pipelines set when a bounded wait gives up; SPMM_ERR_TIMEOUT if it was set. */
+spmm_status spmm_device_error_check(void* stream);
+/* Number of SMs of the current device (for grid sizing in callers). */
+int spmm_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BCSR_SPMM_H */

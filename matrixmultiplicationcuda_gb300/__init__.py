@@ -1,0 +1,58 @@
+"""GB300 (sm_103a) BCSR sparse x dense matrix multiply.
+
+Python access to libbcsr_spmm.so, the C ABI declared in include/bcsr_spmm.h.
+Device memory and streams come from PyTorch; all arithmetic happens in the
+library's own CUDA kernels. There is no CPU fallback: if the shared library is
+missing, importing the compute entry points raises.
+
+The reference-shaped launchers keep the argument lists of the reference's
+kernels (src/cuda_kernels.cuh:39-114): ``sparseMatrixMulTensor(hdr, idx,
+data, B, C, M, N, K)`` and the 32x16 / 64x16 / Adaptive variants.
+"""
+import ctypes
+import os
+
+from ._lib import (  # noqa: F401
+    SpmmError,
+    Status,
+    DType,
+    Config,
+    lib,
+    lib_path,
+    check,
+    stream_handle,
+)
+from .bcsr import (  # noqa: F401
+    BCSR,
+    spmm,
+    sparseMatrixMulTensor,
+    sparseMatrixMulTensor32x16,
+    sparseMatrixMulTensor64x16,
+    sparseMatrixMulTensorAdaptive,
+    sparseMatrixMulTensorAdaptive32x16,
+    sparseMatrixMulTensorAdaptive64x16,
+    dense_to_bcsr,
+    validate,
+    quantize,
+    device_error_check,
+    debug_wait_timeout,
+)
+from .host import (  # noqa: F401
+    generate_matrix,
+    gen_structure,
+    gen_values,
+    gen_dense,
+    host_dense_to_bcsr,
+    host_dense_to_csr,
+    mat_load,
+    mat_save,
+    PATTERN_RANDOM,
+    PATTERN_BAND,
+    PATTERN_BLOCKDIAG,
+    PATTERN_LOGNORMAL,
+    DIST_UNIFORM,
+    DIST_SCALED_NORMAL,
+    DIST_NORMAL,
+)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

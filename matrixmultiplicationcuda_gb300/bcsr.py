@@ -1,0 +1,187 @@
+"""Device-side API: BCSR operands held in torch device tensors, and the calls
+into the library's kernels."""
+import ctypes
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from ._lib import (BcsrDesc, Config, DenseDesc, DType, SpmmError, Status, check, lib,
+                   stream_handle)
+
+_TORCH_DT = None
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t):
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def storage_dtype(dtype):
+    torch = _torch()
+    return {DType.F16: torch.float16, DType.BF16: torch.bfloat16, DType.E4M3: torch.uint8,
+            DType.F16_SPLIT: torch.float16}[DType(dtype)]
+
+
+@dataclass
+class BCSR:
+    """A on the device in the reference's BCSR layout (formats/BCSRMatrix.cuh:9-26).
+
+    row_ptr: int32 [M/bR + 1]; col_idx: int32 [nnzb] in units of 16 columns;
+    vals: [nnzb * bR * bC] blocks row-major (fp16 / bf16 / e4m3 bytes);
+    vals_lo: F16_SPLIT low halves; scales: E4M3 per-block fp32 scales.
+    """
+    M: int
+    K: int
+    bR: int
+    bC: int
+    row_ptr: object
+    col_idx: object
+    vals: object
+    dtype: DType = DType.F16
+    vals_lo: object = None
+    scales: object = None
+
+    @property
+    def nnzb(self):
+        return int(self.col_idx.numel())
+
+    def desc(self):
+        d = BcsrDesc()
+        d.M, d.K, d.bR, d.bC = self.M, self.K, self.bR, self.bC
+        d.row_ptr = self.row_ptr.data_ptr()
+        d.col_idx = self.col_idx.data_ptr() if self.col_idx.numel() else None
+        d.vals = self.vals.data_ptr() if self.vals.numel() else None
+        d.vals_lo = self.vals_lo.data_ptr() if self.vals_lo is not None else None
+        d.scales = self.scales.data_ptr() if self.scales is not None else None
+        d.dtype = int(self.dtype)
+        return d
+
+    @staticmethod
+    def from_host(M, K, bR, row_ptr, col_idx, vals_f32, dtype=DType.F16, device="cuda"):
+        """Upload a host BCSR (fp32 block values) and convert the values to `dtype`
+        on the device with the library's conversion kernels."""
+        torch = _torch()
+        rp = torch.as_tensor(np.ascontiguousarray(row_ptr, np.int32)).to(device)
+        ci = torch.as_tensor(np.ascontiguousarray(col_idx, np.int32)).to(device)
+        v32 = torch.as_tensor(np.ascontiguousarray(vals_f32, np.float32).reshape(-1)).to(device)
+        vals, lo, sc = quantize(v32, dtype, block_elems=bR * 16)
+        return BCSR(M, K, bR, 16, rp, ci, vals, DType(dtype), lo, sc)
+
+
+def _dense_desc(B, B_lo=None, scale=1.0, ldb=None):
+    d = DenseDesc()
+    d.data = B.data_ptr()
+    d.data_lo = B_lo.data_ptr() if B_lo is not None else None
+    d.scale = float(scale)
+    d.ldb = int(ldb if ldb is not None else B.shape[-1])
+    return d
+
+
+def spmm(A: BCSR, B, N=None, C=None, cfg: Optional[Config] = None, stream=None, B_lo=None,
+         b_scale=1.0, ldc=None):
+    """C = A @ B on the device (fp32 C, allocated if not given). Asynchronous."""
+    torch = _torch()
+    N = int(B.shape[1]) if N is None else int(N)
+    if C is None:
+        C = torch.empty((A.M, N), dtype=torch.float32, device=B.device)
+    ldc = int(C.stride(0)) if ldc is None else int(ldc)
+    a = A.desc()
+    b = _dense_desc(B, B_lo, b_scale, ldb=B.stride(0))
+    st = lib().spmm_bcsr_mm(ctypes.byref(a), ctypes.byref(b), N, ctypes.c_void_p(C.data_ptr()),
+                            ldc, ctypes.byref(cfg) if cfg is not None else None,
+                            stream_handle(stream))
+    check(st)
+    return C
+
+
+def _ref_launch(fn, hdr, idx, data, B, C, M, N, K, stream, extra=()):
+    st = fn(_ptr(hdr), _ptr(idx), _ptr(data), _ptr(B), _ptr(C), int(M), int(N), *extra, int(K),
+            stream_handle(stream))
+    check(st)
+    return C
+
+
+# Reference-shaped launchers (src/cuda_kernels.cuh:39-114 argument order, + K, + stream).
+def sparseMatrixMulTensor(hdr, idx, data, B, C, M, N, K, stream=None):
+    return _ref_launch(lib().sparseMatrixMulTensor_launch, hdr, idx, data, B, C, M, N, K, stream)
+
+
+def sparseMatrixMulTensor32x16(hdr, idx, data, B, C, M, N, K, stream=None):
+    return _ref_launch(lib().sparseMatrixMulTensor32x16_launch, hdr, idx, data, B, C, M, N, K, stream)
+
+
+def sparseMatrixMulTensor64x16(hdr, idx, data, B, C, M, N, K, stream=None):
+    return _ref_launch(lib().sparseMatrixMulTensor64x16_launch, hdr, idx, data, B, C, M, N, K, stream)
+
+
+def sparseMatrixMulTensorAdaptive(hdr, idx, data, B, C, M, N, colBlocksPerRow, K, stream=None):
+    return _ref_launch(lib().sparseMatrixMulTensorAdaptive_launch, hdr, idx, data, B, C, M, N, K,
+                       stream, (int(colBlocksPerRow),))
+
+
+def sparseMatrixMulTensorAdaptive32x16(hdr, idx, data, B, C, M, N, colBlocksPerRow, K, stream=None):
+    return _ref_launch(lib().sparseMatrixMulTensorAdaptive32x16_launch, hdr, idx, data, B, C, M, N,
+                       K, stream, (int(colBlocksPerRow),))
+
+
+def sparseMatrixMulTensorAdaptive64x16(hdr, idx, data, B, C, M, N, colBlocksPerRow, K, stream=None):
+    return _ref_launch(lib().sparseMatrixMulTensorAdaptive64x16_launch, hdr, idx, data, B, C, M, N,
+                       K, stream, (int(colBlocksPerRow),))
+
+
+def dense_to_bcsr(A_half, bR=16, bC=16, stream=None):
+    """GPU BCSRMatrix constructor: (row_ptr, col_idx, vals) device tensors, bit-exact
+    to formats/BCSRMatrix.cu:22-74. Synchronises once (to size the outputs)."""
+    torch = _torch()
+    M, K = A_half.shape
+    lda = A_half.stride(0)
+    MB = M // bR
+    rp = torch.empty(MB + 1, dtype=torch.int32, device=A_half.device)
+    nnzb = ctypes.c_longlong(0)
+    s = stream_handle(stream)
+    check(lib().spmm_dense_to_bcsr_count(_ptr(A_half), M, K, lda, bR, bC, _ptr(rp),
+                                         ctypes.byref(nnzb), s))
+    ci = torch.empty(max(nnzb.value, 0), dtype=torch.int32, device=A_half.device)
+    vals = torch.empty(max(nnzb.value, 0) * bR * bC, dtype=torch.float16, device=A_half.device)
+    if nnzb.value:
+        check(lib().spmm_dense_to_bcsr_fill(_ptr(A_half), M, K, lda, bR, bC, _ptr(rp), _ptr(ci),
+                                            _ptr(vals), s))
+    return rp, ci, vals
+
+
+def validate(A: BCSR, stream=None):
+    check(lib().spmm_bcsr_validate(_ptr(A.row_ptr), _ptr(A.col_idx) if A.nnzb else None, A.M, A.K,
+                                   A.bR, A.nnzb, stream_handle(stream)))
+
+
+def quantize(src_f32, dtype, block_elems=None, stream=None):
+    """fp32 device tensor -> (values, low halves or None, scales or None) in `dtype`."""
+    torch = _torch()
+    dtype = DType(dtype)
+    n = src_f32.numel()
+    dev = src_f32.device
+    dst = torch.empty(n, dtype=storage_dtype(dtype), device=dev)
+    lo = torch.empty(n, dtype=torch.float16, device=dev) if dtype == DType.F16_SPLIT else None
+    sc = None
+    be = 0
+    if dtype == DType.E4M3:
+        be = int(block_elems if block_elems else n)
+        sc = torch.empty((n + be - 1) // be if n else 0, dtype=torch.float32, device=dev)
+    if n:
+        check(lib().spmm_quantize(_ptr(src_f32), n, int(dtype), be, _ptr(dst), _ptr(lo), _ptr(sc),
+                                  stream_handle(stream)))
+    return dst, lo, sc
+
+
+def device_error_check(stream=None):
+    check(lib().spmm_device_error_check(stream_handle(stream)))
+
+
+def debug_wait_timeout(timeout_ns, stream=None):
+    """Returns the Status of the bounded-wait diagnostic (TIMEOUT expected)."""
+    return Status(lib().spmm_debug_wait_timeout(int(timeout_ns), stream_handle(stream)))

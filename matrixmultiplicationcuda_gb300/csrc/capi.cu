@@ -1,0 +1,236 @@
+// C ABI of libbcsr_spmm: argument checks, error reporting and dispatch.
+#include <cudaTypedefs.h>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include "internal.h"
+
+namespace spmm {
+
+namespace {
+thread_local std::string g_last_error;
+std::mutex g_mu;
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+constexpr int kMaxDevices = 64;
+unsigned* g_err_word[kMaxDevices] = {nullptr};
+int g_sms[kMaxDevices] = {0};
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) return -1;
+  return d;
+}
+}  // namespace
+
+spmm_status fail(spmm_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+spmm_status host_fail(spmm_status st, const std::string& msg) { return fail(st, msg); }
+
+spmm_status cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return SPMM_ERR_CUDA;
+}
+
+int sm_count() {
+  int d = current_device();
+  if (d < 0 || d >= kMaxDevices) return 1;
+  if (g_sms[d] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
+    g_sms[d] = n > 0 ? n : 1;
+  }
+  return g_sms[d];
+}
+
+unsigned* device_error_word() {
+  int d = current_device();
+  if (d < 0 || d >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_err_word[d]) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, 256) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, 256) != cudaSuccess) return nullptr;
+    g_err_word[d] = static_cast<unsigned*>(p);
+  }
+  return g_err_word[d];
+}
+
+unsigned long long wait_limit_ns() {
+  static unsigned long long v = [] {
+    const char* s = std::getenv("SPMM_WAIT_LIMIT_NS");
+    unsigned long long x = s ? std::strtoull(s, nullptr, 10) : 0ull;
+    return x ? x : 1000000000ull;  // one second
+  }();
+  return v;
+}
+
+spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const void* base,
+                               uint64_t inner, uint64_t outer, uint64_t row_stride_bytes,
+                               uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz) {
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_encode) {
+      cudaDriverEntryPointQueryResult q;
+      void* fn = nullptr;
+      cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                        cudaEnableDefault, &q);
+      if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(SPMM_ERR_CUDA, "cuTensorMapEncodeTiled entry point not available");
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+  }
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {row_stride_bytes};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, dt, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(SPMM_ERR_INVALID_ARG,
+                "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) +
+                    "): B needs a 16-byte aligned base and a row stride that is a multiple of 16 bytes");
+  return SPMM_OK;
+}
+
+}  // namespace spmm
+
+using namespace spmm;
+
+extern "C" {
+
+int spmm_abi_version(void) { return 1; }
+
+const char* spmm_last_error(void) { return g_last_error.c_str(); }
+
+int spmm_device_sm_count(void) { return sm_count(); }
+
+spmm_status spmm_device_error_check(void* stream) {
+  unsigned* w = device_error_word();
+  if (!w) return fail(SPMM_ERR_CUDA, "no device error word");
+  SPMM_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  unsigned v = 0;
+  SPMM_CUDA_TRY(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
+  if (v) {
+    SPMM_CUDA_TRY(cudaMemset(w, 0, sizeof(unsigned)));
+    return fail(SPMM_ERR_TIMEOUT, "a device-side pipeline wait timed out (code " +
+                                      std::to_string(v) + ")");
+  }
+  return SPMM_OK;
+}
+
+spmm_status spmm_bcsr_mm(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N, float* C,
+                         int ldc, const spmm_config* cfg, void* stream) {
+  g_last_error.clear();
+  if (!A || !B) return fail(SPMM_ERR_INVALID_ARG, "null descriptor");
+  if (A->M < 0 || A->K < 0 || N < 0) return fail(SPMM_ERR_INVALID_ARG, "negative size");
+  if (A->bC != 16) return fail(SPMM_ERR_UNSUPPORTED, "block width must be 16");
+  if (A->bR != 16 && A->bR != 32 && A->bR != 64)
+    return fail(SPMM_ERR_UNSUPPORTED, "block height must be 16, 32 or 64");
+  if (A->M % A->bR) return fail(SPMM_ERR_INVALID_ARG, "M must be a multiple of the block height");
+  if (A->K % 16) return fail(SPMM_ERR_INVALID_ARG, "K must be a multiple of 16");
+  if (A->M == 0 || N == 0) return SPMM_OK;
+  if (!A->row_ptr || !C || !B->data) return fail(SPMM_ERR_INVALID_ARG, "null pointer");
+  // col_idx / vals may be NULL only when A stores no blocks (they are never read then)
+  const bool e4m3 = A->dtype == SPMM_E4M3, split = A->dtype == SPMM_F16_SPLIT;
+  if ((int)A->dtype < 0 || (int)A->dtype > 3) return fail(SPMM_ERR_INVALID_ARG, "unknown dtype");
+  if (e4m3 && !A->scales) return fail(SPMM_ERR_INVALID_ARG, "E4M3 needs per-block scales");
+  if (split && (!A->vals_lo || !B->data_lo))
+    return fail(SPMM_ERR_INVALID_ARG, "F16_SPLIT needs the low halves of A and B");
+  const int nmul = e4m3 ? 16 : 8;
+  if (N % nmul) return fail(SPMM_ERR_UNSUPPORTED, "N must be a multiple of " + std::to_string(nmul));
+  if (B->ldb < N || B->ldb % nmul) return fail(SPMM_ERR_MISALIGNED, "ldb must be >= N and a multiple of " + std::to_string(nmul));
+  if (ldc < N || ldc % 4) return fail(SPMM_ERR_MISALIGNED, "ldc must be >= N and a multiple of 4");
+  if (!aligned(A->vals, 16) || !aligned(B->data, 16) || !aligned(C, 16) ||
+      (split && (!aligned(A->vals_lo, 16) || !aligned(B->data_lo, 16))))
+    return fail(SPMM_ERR_MISALIGNED, "A values, B and C must be 16-byte aligned");
+  if (A->K == 0) {
+    // No block columns: C = 0 for the window.
+    SPMM_CUDA_TRY(cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, A->M,
+                                    static_cast<cudaStream_t>(stream)));
+    return SPMM_OK;
+  }
+  LaunchRequest r;
+  r.A = A;
+  r.B = B;
+  r.N = N;
+  r.C = C;
+  r.ldc = ldc;
+  std::memset(&r.cfg, 0, sizeof(r.cfg));
+  if (cfg) r.cfg = *cfg;
+  r.stream = static_cast<cudaStream_t>(stream);
+  if (r.cfg.kernel == 2 || (r.cfg.kernel == 0 && A->bR == 64)) {
+    spmm_status st = launch_tc(r);
+    if (st != SPMM_ERR_UNSUPPORTED || r.cfg.kernel == 2) return st;
+    g_last_error.clear();
+  }
+  return launch_mma(r);
+}
+
+static spmm_status ref_launch(int bR, const int* hdr, const int* idx, const void* data,
+                              const void* B, float* C, unsigned M, unsigned N, unsigned K,
+                              void* stream) {
+  spmm_bcsr_desc a;
+  std::memset(&a, 0, sizeof(a));
+  a.M = (int)M;
+  a.K = (int)K;
+  a.bR = bR;
+  a.bC = 16;
+  a.row_ptr = hdr;
+  a.col_idx = idx;
+  a.vals = data;
+  a.dtype = SPMM_F16;
+  spmm_dense_desc b;
+  std::memset(&b, 0, sizeof(b));
+  b.data = B;
+  b.scale = 1.0f;
+  b.ldb = (int)N;
+  return spmm_bcsr_mm(&a, &b, (int)N, C, (int)N, nullptr, stream);
+}
+
+spmm_status sparseMatrixMulTensor_launch(const int* hdr, const int* idx, const void* data,
+                                         const void* B, float* C, unsigned M, unsigned N,
+                                         unsigned K, void* stream) {
+  return ref_launch(16, hdr, idx, data, B, C, M, N, K, stream);
+}
+spmm_status sparseMatrixMulTensor32x16_launch(const int* hdr, const int* idx, const void* data,
+                                              const void* B, float* C, unsigned M, unsigned N,
+                                              unsigned K, void* stream) {
+  return ref_launch(32, hdr, idx, data, B, C, M, N, K, stream);
+}
+spmm_status sparseMatrixMulTensor64x16_launch(const int* hdr, const int* idx, const void* data,
+                                              const void* B, float* C, unsigned M, unsigned N,
+                                              unsigned K, void* stream) {
+  return ref_launch(64, hdr, idx, data, B, C, M, N, K, stream);
+}
+spmm_status sparseMatrixMulTensorAdaptive_launch(const int* hdr, const int* idx, const void* data,
+                                                 const void* B, float* C, unsigned M, unsigned N,
+                                                 unsigned colBlocksPerRow, unsigned K,
+                                                 void* stream) {
+  (void)colBlocksPerRow;
+  return ref_launch(16, hdr, idx, data, B, C, M, N, K, stream);
+}
+spmm_status sparseMatrixMulTensorAdaptive32x16_launch(const int* hdr, const int* idx,
+                                                      const void* data, const void* B, float* C,
+                                                      unsigned M, unsigned N,
+                                                      unsigned colBlocksPerRow, unsigned K,
+                                                      void* stream) {
+  (void)colBlocksPerRow;
+  return ref_launch(32, hdr, idx, data, B, C, M, N, K, stream);
+}
+spmm_status sparseMatrixMulTensorAdaptive64x16_launch(const int* hdr, const int* idx,
+                                                      const void* data, const void* B, float* C,
+                                                      unsigned M, unsigned N,
+                                                      unsigned colBlocksPerRow, unsigned K,
+                                                      void* stream) {
+  (void)colBlocksPerRow;
+  return ref_launch(64, hdr, idx, data, B, C, M, N, K, stream);
+}
+
+}  // extern "C"

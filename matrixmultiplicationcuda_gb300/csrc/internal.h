@@ -1,0 +1,44 @@
+// Host-side internals shared by the translation units of libbcsr_spmm.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include "../../include/bcsr_spmm.h"
+
+namespace spmm {
+
+// Thread-local last-error text; returns the status for chaining.
+spmm_status fail(spmm_status st, const std::string& msg);
+spmm_status cuda_fail(cudaError_t e, const char* what);
+#define SPMM_CUDA_TRY(expr)                                   \
+  do {                                                        \
+    cudaError_t _e = (expr);                                  \
+    if (_e != cudaSuccess) return ::spmm::cuda_fail(_e, #expr); \
+  } while (0)
+
+int sm_count();                                  // SMs of the current device
+unsigned* device_error_word();                   // per-device error word (lazy)
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point.
+spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const void* base,
+                               uint64_t inner, uint64_t outer, uint64_t row_stride_bytes,
+                               uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz);
+
+struct LaunchRequest {
+  const spmm_bcsr_desc* A;
+  const spmm_dense_desc* B;
+  int N;
+  float* C;
+  long long ldc;
+  spmm_config cfg;
+  cudaStream_t stream;
+};
+// mma.sync family (spmm_mma.cu)
+spmm_status launch_mma(const LaunchRequest& r);
+// tcgen05 family (spmm_tc.cu); returns SPMM_ERR_UNSUPPORTED when it has no kernel for r
+spmm_status launch_tc(const LaunchRequest& r);
+
+unsigned long long wait_limit_ns();              // bounded-wait limit for device waits
+
+}  // namespace spmm
