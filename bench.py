@@ -430,8 +430,38 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line))
 
 
+def run_profile(args):
+    """One problem copy, `--launches` launches of one precision / configuration and
+    nothing else: the command the ncu captures in profiles/ run."""
+    import torch
+    import matrixmultiplicationcuda_gb300 as m
+    from matrixmultiplicationcuda_gb300 import DType
+    dev = torch.device("cuda", 0)
+    rp, ci = make_structure()
+    nnzb = len(ci)
+    vals = m.gen_values(nnzb, BR, 16, m.DIST_SCALED_NORMAL, seed=SEED + 1)
+    Bf = m.gen_dense(K, N, m.DIST_NORMAL, seed=SEED + 2)
+    dt = {"f16": DType.F16, "bf16": DType.BF16, "e4m3": DType.E4M3, "f16_split": DType.F16_SPLIT}[args.profile]
+    qv, qlo, qs = m.quantize(torch.from_numpy(vals).to(dev), dt, block_elems=BR * 16)
+    Bq, Blo, Bs = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), dt)
+    A = m.BCSR(M, K, BR, 16, torch.from_numpy(rp).to(dev), torch.from_numpy(ci).to(dev), qv, dt, qlo, qs)
+    C = torch.empty((M, N), dtype=torch.float32, device=dev)
+    cfg = m.Config(kernel=args.kernel, n_tile=args.n_tile, stages=args.stages)
+    for _ in range(args.launches):
+        m.spmm(A, Bq.view(K, N), N=N, C=C, cfg=cfg, B_lo=Blo.view(K, N) if Blo is not None else None,
+               b_scale=float(Bs[0]) if Bs is not None else 1.0)
+    torch.cuda.synchronize()
+    m.device_error_check()
+    print("profile: %s nnzb=%d launches=%d" % (args.profile, nnzb, args.launches))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile", default=None, choices=["f16", "bf16", "e4m3", "f16_split"])
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--kernel", type=int, default=0)
+    ap.add_argument("--n-tile", type=int, default=0)
+    ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
@@ -441,7 +471,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_ours(args, world, rank, local)
