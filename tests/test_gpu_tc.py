@@ -1,0 +1,55 @@
+"""The tcgen05 (UMMA + TMEM) pipeline against the FP64 oracle, every
+instantiated (block height, column tile, precision), including empty block
+rows, partial column tiles and poisoned outputs.
+
+Bars: fp16 / bf16 inputs rounded first, so the FP64 product of the rounded
+values is the reference and only fp32 accumulation order differs:
+normwise error <= 1e-5. Split fp16 hi+lo against the fp32 values: <= 2e-6.
+"""
+import numpy as np
+import pytest
+import torch
+
+import matrixmultiplicationcuda_gb300 as m
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(64, 128, "f16"), (64, 256, "f16"), (64, 512, "f16"), (32, 256, "f16"), (16, 256, "f16"),
+         (64, 128, "bf16"), (64, 256, "bf16"), (64, 512, "bf16"), (32, 256, "bf16"), (16, 256, "bf16"),
+         (64, 256, "split"), (64, 128, "split")]
+DT = {"f16": m.DType.F16, "bf16": m.DType.BF16, "split": m.DType.F16_SPLIT}
+
+
+def rounded(x, name):
+    t = torch.from_numpy(x)
+    if name == "f16":
+        return t.half().double().numpy()
+    if name == "bf16":
+        return t.bfloat16().double().numpy()
+    return x.astype(np.float64)
+
+
+@pytest.mark.parametrize("bR,nt,name", CASES)
+@pytest.mark.parametrize("N", [64, 200, 512])
+def test_tc_matches_fp64(dev, bR, nt, name, N):
+    N = N - N % 8
+    M, K = 512, 1024
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, 0.06, 1.5, seed=bR + N)
+    vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=3)
+    Bf = m.gen_dense(K, N, m.DIST_UNIFORM, seed=4)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, DT[name], device=dev)
+    Bq, Blo, _ = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), DT[name])
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    m.spmm(A, Bq.view(K, N), N=N, C=C, B_lo=Blo.view(K, N) if Blo is not None else None,
+           cfg=m.Config(kernel=2, n_tile=nt))
+    m.device_error_check()
+    got = C.cpu().numpy()
+    ref = oracle.bcsr_matmul_f64(rp, ci, rounded(vals, name), bR, 16, rounded(Bf, name))
+    assert np.isfinite(got).all()
+    mx, fr = oracle.rel_errors(got, ref)
+    bar = 2e-6 if name == "split" else 1e-5
+    assert mx <= bar and fr <= bar, (mx, fr)
+    empty = np.nonzero(np.diff(rp) == 0)[0]
+    for br in empty[:4]:
+        assert np.all(got[br * bR:(br + 1) * bR] == 0)
