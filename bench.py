@@ -297,7 +297,7 @@ def run_ours(args, world, rank, local):
 
     # autotune every precision over the instantiated kernel configurations
     cands = [m.Config(kernel=k, n_tile=nt, stages=st) for k, nt, st in
-             [(2, 0, 0), (1, 128, 4), (1, 128, 8), (1, 64, 4), (1, 256, 4)]]
+             [(2, 128, 0), (2, 256, 0), (2, 512, 0), (1, 128, 4), (1, 128, 8), (1, 64, 4), (1, 256, 4)]]
     results = {}
     prepared = {}
     sampler = ClockSampler(local)
@@ -314,6 +314,7 @@ def run_ours(args, world, rank, local):
             except m.SpmmError:
                 continue
             t = time_loop(probs, cfg, 30)
+            sys.stderr.write("tune %s kernel=%d n_tile=%d stages=%d: %.2f us\n" % (name, cfg.kernel, cfg.n_tile, cfg.stages, t * 1e3))
             if best is None or t < best[0]:
                 best = (t, cfg)
         results[name] = {"ms": best[0], "cfg": best[1], "tflops": flops / best[0] / 1e9,
