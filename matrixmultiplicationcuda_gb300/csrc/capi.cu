@@ -99,6 +99,25 @@ spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const v
   return SPMM_OK;
 }
 
+spmm_status encode_panel_map_3d(CUtensorMap* map, const void* base, uint64_t N, uint64_t K,
+                                uint64_t row_stride_bytes, uint32_t boxes) {
+  if (N % 64 || boxes == 0 || boxes > 256) return fail(SPMM_ERR_UNSUPPORTED, "panel map needs N % 64 == 0");
+  CUtensorMap probe;
+  spmm_status st = encode_tile_map_2d(&probe, CU_TENSOR_MAP_DATA_TYPE_UINT16, base, N, K, row_stride_bytes,
+                                      64, 16, CU_TENSOR_MAP_SWIZZLE_128B);   // resolves the entry point
+  if (st != SPMM_OK) return st;
+  cuuint64_t dims[3] = {64, K, N / 64};
+  cuuint64_t strides[2] = {row_stride_bytes, 128};
+  cuuint32_t box[3] = {64, 16, boxes};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void*>(base), dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(SPMM_ERR_UNSUPPORTED, "3-D panel tensor map rejected (" + std::to_string((int)r) + ")");
+  return SPMM_OK;
+}
+
 }  // namespace spmm
 
 using namespace spmm;

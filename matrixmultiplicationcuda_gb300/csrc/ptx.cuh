@@ -1,7 +1,9 @@
 // Inline-PTX helpers for sm_103a: mbarriers, TMA bulk / tensor copies,
-// ldmatrix and mma.sync. Every wait is bounded by a wall-clock limit read from
-// %globaltimer; a wait that runs out returns false and the caller records an
-// error and leaves, so no kernel here can spin forever.
+// ldmatrix and mma.sync. Every wait is bounded: a wait that runs out returns
+// false and the caller records an error and leaves, so no kernel here can spin
+// forever. The bound is counted in SM clock cycles (clock64, a few cycles to
+// read); %globaltimer costs hundreds of nanoseconds per read, which on a
+// producer/consumer hand-off path costs more than the TMA copy it waits for.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -44,12 +46,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase with the given parity to complete.
+// Bounded wait for the phase with the given parity to complete. The limit is
+// given in nanoseconds and applied as SM cycles at 2 cycles per nanosecond
+// (the SM clock is at most 2.07 GHz, so the real bound is about limit_ns).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = global_timer_ns();
+  const long long t0 = clock64();
+  const long long limit = (long long)(limit_ns * 2ull);
   while (!mbar_try_wait(bar, parity)) {
-    if (global_timer_ns() - t0 > limit_ns) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -71,6 +76,15 @@ __device__ __forceinline__ void tma_tile_2d_g2s(uint32_t dst, const void* tmap, 
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       ".L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
       "l"(tmap), "r"(x), "r"(y), "r"(bar), "l"(policy)
+      : "memory");
+}
+// Tiled 3-D tensor copy global -> shared; {x, y, z} innermost first.
+__device__ __forceinline__ void tma_tile_3d_g2s(uint32_t dst, const void* tmap, int x, int y, int z,
+                                                uint32_t bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      ".L2::cache_hint [%0], [%1, {%2, %3, %4}], [%5], %6;" ::"r"(dst),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(bar), "l"(policy)
       : "memory");
 }
 __device__ __forceinline__ void tma_prefetch_desc(const void* tmap) {

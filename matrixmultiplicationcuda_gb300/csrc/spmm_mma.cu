@@ -1,4 +1,6 @@
 // Instantiations and host dispatch of the mma.sync BCSR pipeline.
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 #include "internal.h"
@@ -98,13 +100,22 @@ spmm_status launch_mma(const LaunchRequest& r) {
   CUtensorMap tmB, tmBlo;
   std::memset(&tmBlo, 0, sizeof(tmBlo));
   const CUtensorMapDataType dt = e4m3 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
-  spmm_status st = encode_tile_map_2d(&tmB, dt, B.data, (uint64_t)r.N, (uint64_t)A.K,
-                                      (uint64_t)B.ldb * esz, 128 / esz, 16,
-                                      CU_TENSOR_MAP_SWIZZLE_128B);
-  if (st != SPMM_OK) return st;
+  // 16-bit B panels: one 3-D copy per panel when N is a multiple of 64.
+  int panel3d = (!e4m3 && r.N % 64 == 0) ? 1 : 0;
+  spmm_status st = SPMM_OK;
+  if (panel3d && encode_panel_map_3d(&tmB, B.data, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * 2,
+                                     (uint32_t)(nt / 64)) != SPMM_OK)
+    panel3d = 0;
+  if (!panel3d) {
+    st = encode_tile_map_2d(&tmB, dt, B.data, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * esz,
+                            128 / esz, 16, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (st != SPMM_OK) return st;
+  }
   if (mode == MODE_SPLIT) {
-    st = encode_tile_map_2d(&tmBlo, dt, B.data_lo, (uint64_t)r.N, (uint64_t)A.K,
-                            (uint64_t)B.ldb * esz, 128 / esz, 16, CU_TENSOR_MAP_SWIZZLE_128B);
+    st = panel3d ? encode_panel_map_3d(&tmBlo, B.data_lo, (uint64_t)r.N, (uint64_t)A.K,
+                                       (uint64_t)B.ldb * 2, (uint32_t)(nt / 64))
+                 : encode_tile_map_2d(&tmBlo, dt, B.data_lo, (uint64_t)r.N, (uint64_t)A.K,
+                                      (uint64_t)B.ldb * esz, 128 / esz, 16, CU_TENSOR_MAP_SWIZZLE_128B);
     if (st != SPMM_OK) return st;
   } else {
     tmBlo = tmB;
@@ -125,6 +136,7 @@ spmm_status launch_mma(const LaunchRequest& r) {
   p.b_scale = B.scale;
   p.timeout_ns = wait_limit_ns();
   p.err = device_error_word();
+  p.panel3d = panel3d;
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
 
@@ -138,6 +150,9 @@ spmm_status launch_mma(const LaunchRequest& r) {
   }
   long long grid = (long long)sm_count() * per_sm;
   if (grid > p.n_items) grid = p.n_items;
+  if (std::getenv("SPMM_DEBUG"))
+    std::fprintf(stderr, "[spmm] mma.sync bR=%d nt=%d stages=%d smem=%zu per_sm=%d grid=%lld items=%d\n",
+                 A.bR, nt, e->stages, e->smem, per_sm, grid, p.n_items);
   e->fn<<<(unsigned)grid, e->threads, e->smem, r.stream>>>(tmB, tmBlo, p);
   SPMM_CUDA_TRY(cudaGetLastError());
   return SPMM_OK;

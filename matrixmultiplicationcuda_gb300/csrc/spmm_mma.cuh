@@ -40,6 +40,7 @@ struct MmaParams {
   float b_scale;   // E4M3: scale of B
   unsigned long long timeout_ns;
   unsigned* err;   // device error word (bit 0: consumer wait timed out, bit 1: producer)
+  int panel3d;     // 16-bit B panel loaded by one 3-D copy (N % 64 == 0)
 };
 
 template <int BR, int NT, int WM, int WN, int STAGES, int MODE>
@@ -63,7 +64,7 @@ struct MmaCfg {
   static constexpr int kMT = kWTM / 16;
   static constexpr int kNT8 = kWTN / 8;
   static constexpr size_t kSmem = 1024 /*align slack*/ + (size_t)STAGES * (kStageB + kStageA) +
-                                  (size_t)STAGES * 16 /*barriers*/;
+                                  (size_t)STAGES * 16 /*barriers*/ + 128 /*column staging*/;
   static_assert(BR % (16 * WM) == 0, "warp rows");
   static_assert(NT % (WN * (MODE == MODE_E4M3 ? 32 : 16)) == 0, "warp cols");
   static_assert(NT % kBoxCols == 0, "box cols");
@@ -95,6 +96,10 @@ __global__ void __launch_bounds__(MmaCfg<BR, NT, WM, WN, STAGES, MODE>::kThreads
 
   if (warp == Cfg::kConsumerWarps) {
     // ------------------------------ producer warp ------------------------------
+    // Lane 0 issues every copy; the other lanes stage column indices 32 at a time
+    // in shared memory and prefetch the next item's row range, so the issuing
+    // lane never waits on a global load or a shuffle between two blocks.
+    int* s_cols = reinterpret_cast<int*>(bars + 2 * STAGES);
     if (lane == 0) {
       tma_prefetch_desc(&tmB);
       if (Cfg::kSplit) tma_prefetch_desc(&tmBlo);
@@ -102,33 +107,49 @@ __global__ void __launch_bounds__(MmaCfg<BR, NT, WM, WN, STAGES, MODE>::kThreads
     const uint64_t pol_b = l2_policy_evict_last();    // B panels are re-read by other rows
     const uint64_t pol_a = l2_policy_evict_first();   // A blocks are read once per column tile
     uint32_t g = 0;
-    for (int item = blockIdx.x; item < p.n_items; item += gridDim.x) {
-      const int br = item / p.ntiles, nt = item - br * p.ntiles;
-      const int start = __ldg(p.row_ptr + br), end = __ldg(p.row_ptr + br + 1);
-      for (int base = start; base < end; base += 32) {
+    int failed = 0;
+    int item = blockIdx.x;
+    int br = item / p.ntiles;
+    int start = item < p.n_items ? __ldg(p.row_ptr + br) : 0;
+    int end = item < p.n_items ? __ldg(p.row_ptr + br + 1) : 0;
+    int mycol = (item < p.n_items && lane < end - start) ? __ldg(p.col_idx + start + lane) : 0;
+    for (; item < p.n_items && !failed; item += gridDim.x) {
+      const int nt = item - br * p.ntiles;
+      const int nitem = item + gridDim.x;
+      const int nbr = nitem / p.ntiles;
+      const int nstart = nitem < p.n_items ? __ldg(p.row_ptr + nbr) : 0;
+      const int nend = nitem < p.n_items ? __ldg(p.row_ptr + nbr + 1) : 0;
+      for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
-        const int mycol = (lane < cnt) ? __ldg(p.col_idx + base + lane) : 0;
-        for (int i = 0; i < cnt; ++i, ++g) {
-          const int col = __shfl_sync(0xffffffffu, mycol, i);
-          const int s = (int)(g % STAGES);
-          int failed = 0;
-          if (lane == 0) {
-            bool ok = true;
-            if (g >= (uint32_t)STAGES)
-              ok = mbar_wait(empty0 + 8 * s, ((g / STAGES) + 1) & 1, p.timeout_ns);
-            if (!ok) {
+        s_cols[lane] = mycol;
+        __syncwarp();
+        const bool more = base + 32 < end;
+        const int nb = more ? base + 32 : nstart;
+        const int nn = more ? end : nend;
+        mycol = (lane < nn - nb && (more || nitem < p.n_items)) ? __ldg(p.col_idx + nb + lane) : 0;
+        if (lane == 0) {
+          for (int i = 0; i < cnt; ++i, ++g) {
+            const int s = (int)(g % STAGES);
+            if (g >= (uint32_t)STAGES &&
+                !mbar_wait(empty0 + 8 * s, ((g / STAGES) + 1) & 1, p.timeout_ns)) {
               atomicOr(p.err, 2u);
               failed = 1;
-            } else {
-              const uint32_t fb = full0 + 8 * s;
-              mbar_arrive_expect_tx(fb, Cfg::kTxBytes);
-              const size_t aoff = (size_t)(base + i) * Cfg::kABytes;
-              uint8_t* a_dst = sA + (size_t)s * Cfg::kStageA;
-              tma_bulk_g2s(smem_u32(a_dst), p.vals + aoff, Cfg::kABytes, fb, pol_a);
+              break;
+            }
+            const int col = s_cols[i];
+            const uint32_t fb = full0 + 8 * s;
+            mbar_arrive_expect_tx(fb, Cfg::kTxBytes);
+            const size_t aoff = (size_t)(base + i) * Cfg::kABytes;
+            uint8_t* a_dst = sA + (size_t)s * Cfg::kStageA;
+            tma_bulk_g2s(smem_u32(a_dst), p.vals + aoff, Cfg::kABytes, fb, pol_a);
+            if (Cfg::kSplit)
+              tma_bulk_g2s(smem_u32(a_dst + Cfg::kABytes), p.vals_lo + aoff, Cfg::kABytes, fb, pol_a);
+            uint8_t* b_dst = sB + (size_t)s * Cfg::kStageB;
+            if (MODE != MODE_E4M3 && p.panel3d) {
+              tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, col * 16, nt * Cfg::kNBox, fb, pol_b);
               if (Cfg::kSplit)
-                tma_bulk_g2s(smem_u32(a_dst + Cfg::kABytes), p.vals_lo + aoff, Cfg::kABytes, fb,
-                             pol_a);
-              uint8_t* b_dst = sB + (size_t)s * Cfg::kStageB;
+                tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, col * 16, nt * Cfg::kNBox, fb, pol_b);
+            } else {
 #pragma unroll
               for (int b = 0; b < Cfg::kNBox; ++b) {
                 tma_tile_2d_g2s(smem_u32(b_dst + b * Cfg::kBoxBytes), &tmB,
@@ -139,10 +160,15 @@ __global__ void __launch_bounds__(MmaCfg<BR, NT, WM, WN, STAGES, MODE>::kThreads
               }
             }
           }
-          // a failed wait ends the producer; the consumers then time out too
-          if (__shfl_sync(0xffffffffu, failed, 0)) return;
         }
+        failed = __shfl_sync(0xffffffffu, failed, 0);
+        __syncwarp();
       }
+      if (start >= end)
+        mycol = (nitem < p.n_items && lane < nend - nstart) ? __ldg(p.col_idx + nstart + lane) : 0;
+      br = nbr;
+      start = nstart;
+      end = nend;
     }
     return;
   }

@@ -17,14 +17,20 @@
 //   * the A block (bR rows x 16) as one box with 32-byte swizzle -- the MMA's
 //     B operand in the K-major canonical layout (8-row groups 256 B apart).
 //
-// Warp roles (192 threads): warp 0 streams TMA copies into a STAGES-deep
-// mbarrier ring; warp 1 (one thread) issues the UMMAs, releases each ring slot
-// with tcgen05.commit and hands finished accumulators to the epilogue; warps
-// 2-5 drain TMEM (double-buffered, so the next item's MMAs overlap) with
-// tcgen05.ld and store C with streaming stores. The grid is persistent over
+// Warp roles (256 threads, two CTAs per SM): warp 0 streams TMA copies into a
+// STAGES-deep mbarrier ring (one copy for the A block and, when N % 64 == 0,
+// one 3-D copy for the whole B panel: a TMA instruction holds its issuing thread
+// for tens of cycles, so copies per block bound the block rate); warp 1 (one
+// thread) issues the UMMAs, releases each ring slot with tcgen05.commit and
+// hands finished accumulators to the epilogue; warp 2 owns the TMEM
+// allocation; warps 4-7 drain TMEM (double-buffered, so the next item's MMAs
+// overlap) with tcgen05.ld and store C with streaming stores. The grid is persistent over
 // items = (block row, NT-column tile). Every mbarrier wait is bounded; a wait
 // that gives up sets the device error word, all roles leave their loops, and
 // the allocating warp frees TMEM after the MMA thread has drained its commits.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include "internal.h"
 #include "ptx.cuh"
@@ -43,6 +49,7 @@ struct TcParams {
   int n_items;
   unsigned long long timeout_ns;
   unsigned* err;
+  int panel3d;      // B panel loaded by one 3-D copy (N % 64 == 0)
 };
 
 template <int BR, int NT, int STAGES, int MODE>
@@ -59,7 +66,7 @@ struct TcCfg {
   static constexpr int kTx = kPanelBytes * kParts + kABytes * kParts;
   static constexpr int kAccCols = kJ * BR;            // TMEM columns of one accumulator
   static constexpr int kTmemCols = (2 * kAccCols) < 32 ? 32 : 2 * kAccCols;
-  static constexpr size_t kSmem = 1024 + (size_t)STAGES * (kStageB + kStageA) + 256;
+  static constexpr size_t kSmem = 1024 + (size_t)STAGES * (kStageB + kStageA) + 512;
   static_assert((kTmemCols & (kTmemCols - 1)) == 0 && kTmemCols <= 512, "TMEM columns");
   static_assert(NT % 128 == 0, "NT");
   // kind::f16 instruction descriptor: D f32, A/B f16 or bf16, A MN-major, B K-major,
@@ -111,7 +118,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 template <int BR, int NT, int STAGES, int MODE>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(256, 2)
     k_bcsr_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
               const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
               const TcParams p) {
@@ -122,10 +129,12 @@ __global__ void __launch_bounds__(192, 1)
   uint8_t* sB = smem;
   uint8_t* sA = smem + (size_t)STAGES * Cfg::kStageB;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sA + (size_t)STAGES * Cfg::kStageA);
-  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done; then the TMEM address
+  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done; then the TMEM
+  // address and the producer's column-index staging buffer
   const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES;
   const uint32_t tfull0 = empty0 + 8 * STAGES, tempty0 = tfull0 + 16, done_bar = tempty0 + 16;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  int* s_cols = reinterpret_cast<int*>(tmem_slot + 1);    // 32 entries
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 32) {
@@ -140,7 +149,7 @@ __global__ void __launch_bounds__(192, 1)
     mbar_init(done_bar, 1);
     fence_mbar_init();
   }
-  if (warp == 0) {
+  if (warp == 2) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(Cfg::kTmemCols)
@@ -154,6 +163,9 @@ __global__ void __launch_bounds__(192, 1)
 
   if (warp == 0) {
     // ------------------------------ TMA producer ---------------------------------
+    // Lane 0 issues every copy; the other lanes fetch column indices 32 at a time
+    // into s_cols and prefetch the next item's row range, so the issuing lane
+    // never waits on a global load or a shuffle between two blocks.
     if (lane == 0) {
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
@@ -161,29 +173,49 @@ __global__ void __launch_bounds__(192, 1)
     const uint64_t pol_b = l2_policy_evict_last();
     const uint64_t pol_a = l2_policy_evict_first();
     uint32_t g = 0;
-    bool failed = false;
-    for (int item = blockIdx.x; item < p.n_items && !failed; item += gridDim.x) {
-      const int br = item / p.ntiles, nt = item - br * p.ntiles;
-      const int start = __ldg(p.row_ptr + br), end = __ldg(p.row_ptr + br + 1);
+    int failed = 0;
+    int item = blockIdx.x;
+    int br = item / p.ntiles;
+    int start = item < p.n_items ? __ldg(p.row_ptr + br) : 0;
+    int end = item < p.n_items ? __ldg(p.row_ptr + br + 1) : 0;
+    int mycol = (item < p.n_items && lane < end - start) ? __ldg(p.col_idx + start + lane) : 0;
+    for (; item < p.n_items && !failed; item += gridDim.x) {
+      const int nt = item - br * p.ntiles;
+      // next item's row range, loaded now and used after this item's copies
+      const int nitem = item + gridDim.x;
+      const int nbr = nitem / p.ntiles;
+      const int nstart = nitem < p.n_items ? __ldg(p.row_ptr + nbr) : 0;
+      const int nend = nitem < p.n_items ? __ldg(p.row_ptr + nbr + 1) : 0;
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
-        const int mycol = (lane < cnt) ? __ldg(p.col_idx + base + lane) : 0;
-        for (int i = 0; i < cnt; ++i, ++g) {
-          const int col = __shfl_sync(0xffffffffu, mycol, i);
-          const int s = (int)(g % STAGES);
-          int bad = 0;
-          if (lane == 0) {
+        s_cols[lane] = mycol;
+        __syncwarp();
+        // column indices of the next chunk (this item's, else the next item's first)
+        const bool more = base + 32 < end;
+        const int nb = more ? base + 32 : nstart;
+        const int nn = more ? end : nend;
+        mycol = (lane < nn - nb && (more || nitem < p.n_items)) ? __ldg(p.col_idx + nb + lane) : 0;
+        if (lane == 0) {
+          for (int i = 0; i < cnt; ++i, ++g) {
+            const int s = (int)(g % STAGES);
             if (g >= (uint32_t)STAGES && !mbar_wait(empty0 + 8 * s, ((g / STAGES) + 1) & 1, p.timeout_ns)) {
               atomicOr(p.err, 4u);
-              bad = 1;
-            } else {
-              const uint32_t fb = full0 + 8 * s;
-              mbar_arrive_expect_tx(fb, Cfg::kTx);
-              uint8_t* a_dst = sA + (size_t)s * Cfg::kStageA;
-              tma_tile_2d_g2s(smem_u32(a_dst), &tmA, 0, (base + i) * BR, fb, pol_a);
+              failed = 1;
+              break;
+            }
+            const int col = s_cols[i];
+            const uint32_t fb = full0 + 8 * s;
+            mbar_arrive_expect_tx(fb, Cfg::kTx);
+            uint8_t* a_dst = sA + (size_t)s * Cfg::kStageA;
+            tma_tile_2d_g2s(smem_u32(a_dst), &tmA, 0, (base + i) * BR, fb, pol_a);
+            if (Cfg::kSplit)
+              tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kABytesPad), &tmAlo, 0, (base + i) * BR, fb, pol_a);
+            uint8_t* b_dst = sB + (size_t)s * Cfg::kStageB;
+            if (p.panel3d) {
+              tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, col * 16, nt * (NT / 64), fb, pol_b);
               if (Cfg::kSplit)
-                tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kABytesPad), &tmAlo, 0, (base + i) * BR, fb, pol_a);
-              uint8_t* b_dst = sB + (size_t)s * Cfg::kStageB;
+                tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, col * 16, nt * (NT / 64), fb, pol_b);
+            } else {
 #pragma unroll
               for (int b = 0; b < NT / 64; ++b) {
                 tma_tile_2d_g2s(smem_u32(b_dst + b * Cfg::kBoxBytes), &tmB, nt * NT + b * 64, col * 16, fb, pol_b);
@@ -193,21 +225,30 @@ __global__ void __launch_bounds__(192, 1)
               }
             }
           }
-          if (__shfl_sync(0xffffffffu, bad, 0)) {
-            failed = true;
-            break;
-          }
         }
+        failed = __shfl_sync(0xffffffffu, failed, 0);
+        __syncwarp();
       }
+      if (start >= end) {
+        // empty row: the prefetch above did not run; fetch the next item's first chunk
+        mycol = (nitem < p.n_items && lane < nend - nstart) ? __ldg(p.col_idx + nstart + lane) : 0;
+      }
+      br = nbr;
+      start = nstart;
+      end = nend;
     }
   } else if (warp == 1) {
     // ------------------------------ MMA issuer -----------------------------------
     if (lane == 0) {
       uint32_t g = 0, it = 0;
       bool failed = false;
-      for (int item = blockIdx.x; item < p.n_items && !failed; item += gridDim.x, ++it) {
-        const int br = item / p.ntiles;
-        const int start = __ldg(p.row_ptr + br), end = __ldg(p.row_ptr + br + 1);
+      int item = blockIdx.x;
+      int start = item < p.n_items ? __ldg(p.row_ptr + item / p.ntiles) : 0;
+      int end = item < p.n_items ? __ldg(p.row_ptr + item / p.ntiles + 1) : 0;
+      for (; item < p.n_items && !failed; item += gridDim.x, ++it) {
+        const int nitem = item + gridDim.x;
+        const int nstart = nitem < p.n_items ? __ldg(p.row_ptr + nitem / p.ntiles) : 0;
+        const int nend = nitem < p.n_items ? __ldg(p.row_ptr + nitem / p.ntiles + 1) : 0;
         const uint32_t acc = it & 1;
         if (it >= 2 && !mbar_wait(tempty0 + 8 * acc, ((it >> 1) + 1) & 1, p.timeout_ns)) {
           atomicOr(p.err, 8u);
@@ -243,14 +284,16 @@ __global__ void __launch_bounds__(192, 1)
         }
         if (failed) break;
         umma_commit(tfull0 + 8 * acc);   // accumulator ready (immediately, for an empty row)
+        start = nstart;
+        end = nend;
       }
       // every MMA this thread issued has completed before TMEM is released
       umma_commit(done_bar);
       if (!mbar_wait(done_bar, 0, p.timeout_ns)) atomicOr(p.err, 8u);
     }
     __syncwarp();
-  } else {
-    // ------------------------------ epilogue (warps 2-5) ---------------------------
+  } else if (warp >= 4) {
+    // ------------------------------ epilogue (warps 4-7) ---------------------------
     const int q = warp & 3;                 // TMEM lane quarter this warp may access
     uint32_t it = 0;
     for (int item = blockIdx.x; item < p.n_items; item += gridDim.x, ++it) {
@@ -263,7 +306,7 @@ __global__ void __launch_bounds__(192, 1)
       }
       tc_fence_after();
       const long long row0 = (long long)br * BR;
-#pragma unroll
+#pragma unroll 1
       for (int j = 0; j < Cfg::kJ; ++j) {
         const int n = nt * NT + j * 128 + q * 32 + lane;
         float* cptr = p.C + row0 * p.ldc + n;
@@ -292,7 +335,7 @@ __global__ void __launch_bounds__(192, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) {
+  if (warp == 2) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols)
                  : "memory");
   }
@@ -312,6 +355,8 @@ struct TcEntry {
 const TcEntry kTcEntries[] = {
     SPMM_TC_ENTRY(64, 128, 8, MODE_F16),   SPMM_TC_ENTRY(64, 256, 6, MODE_F16),
     SPMM_TC_ENTRY(64, 512, 6, MODE_F16),   SPMM_TC_ENTRY(32, 256, 8, MODE_F16),
+    SPMM_TC_ENTRY(64, 128, 16, MODE_F16),  SPMM_TC_ENTRY(64, 256, 10, MODE_F16),
+    SPMM_TC_ENTRY(64, 256, 4, MODE_F16),   SPMM_TC_ENTRY(64, 512, 10, MODE_F16),
     SPMM_TC_ENTRY(16, 256, 8, MODE_F16),   SPMM_TC_ENTRY(64, 128, 8, MODE_BF16),
     SPMM_TC_ENTRY(64, 256, 6, MODE_BF16),  SPMM_TC_ENTRY(64, 512, 6, MODE_BF16),
     SPMM_TC_ENTRY(32, 256, 8, MODE_BF16),  SPMM_TC_ENTRY(16, 256, 8, MODE_BF16),
@@ -346,9 +391,17 @@ spmm_status launch_tc(const LaunchRequest& r) {
   spmm_status st = encode_tile_map_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals, 16, rows_bound, 32,
                                       16, (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
   if (st != SPMM_OK) return st;
-  st = encode_tile_map_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data, (uint64_t)r.N, (uint64_t)A.K,
-                          (uint64_t)B.ldb * 2, 64, 16, CU_TENSOR_MAP_SWIZZLE_128B);
-  if (st != SPMM_OK) return st;
+  // B panels: one 3-D copy per panel when N is a multiple of 64, else one 2-D
+  // copy per 64-column box.
+  int panel3d = (r.N % 64 == 0 && r.cfg.kernel != 3) ? 1 : 0;
+  if (panel3d && encode_panel_map_3d(&tmB, B.data, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * 2,
+                                     (uint32_t)(nt / 64)) != SPMM_OK)
+    panel3d = 0;
+  if (!panel3d) {
+    st = encode_tile_map_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data, (uint64_t)r.N, (uint64_t)A.K,
+                            (uint64_t)B.ldb * 2, 64, 16, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (st != SPMM_OK) return st;
+  }
   tmAlo = tmA;
   tmBlo = tmB;
   if (mode == MODE_SPLIT) {
@@ -356,8 +409,10 @@ spmm_status launch_tc(const LaunchRequest& r) {
     st = encode_tile_map_2d(&tmAlo, CU_TENSOR_MAP_DATA_TYPE_UINT16, lo, 16, rows_bound, 32, 16,
                             (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
     if (st != SPMM_OK) return st;
-    st = encode_tile_map_2d(&tmBlo, CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data_lo, (uint64_t)r.N,
-                            (uint64_t)A.K, (uint64_t)B.ldb * 2, 64, 16, CU_TENSOR_MAP_SWIZZLE_128B);
+    st = panel3d ? encode_panel_map_3d(&tmBlo, B.data_lo, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * 2,
+                                       (uint32_t)(nt / 64))
+                 : encode_tile_map_2d(&tmBlo, CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data_lo, (uint64_t)r.N,
+                                      (uint64_t)A.K, (uint64_t)B.ldb * 2, 64, 16, CU_TENSOR_MAP_SWIZZLE_128B);
     if (st != SPMM_OK) return st;
   }
   TcParams p;
@@ -370,20 +425,29 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.n_items = (A.M / A.bR) * p.ntiles;
   p.timeout_ns = wait_limit_ns();
   p.err = device_error_word();
+  p.panel3d = panel3d;
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
   SPMM_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(e->fn),
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
-  int per_sm = 0;
-  SPMM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(e->fn),
-                                                              192, e->smem));
+  // CTAs per SM from the real limits: TMEM columns (512 per SM), shared memory
+  // per SM, and the two CTAs the launch bounds budget registers for. (The
+  // runtime's occupancy query reports one CTA per SM for this kernel, while two
+  // run side by side.)
+  int dev = 0, smem_sm = 0;
+  SPMM_CUDA_TRY(cudaGetDevice(&dev));
+  SPMM_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   const int tmem_fit = 512 / e->tmem_cols;
-  if (per_sm > tmem_fit) per_sm = tmem_fit;
+  const int smem_fit = smem_sm / (int)(e->smem + 1024);
+  int per_sm = std::min(2, std::min(tmem_fit, smem_fit));
   if (r.cfg.ctas_per_sm > 0 && r.cfg.ctas_per_sm < per_sm) per_sm = r.cfg.ctas_per_sm;
   if (per_sm < 1) per_sm = 1;
   long long grid = (long long)sm_count() * per_sm;
   if (grid > p.n_items) grid = p.n_items;
-  e->fn<<<(unsigned)grid, 192, e->smem, r.stream>>>(tmA, tmAlo, tmB, tmBlo, p);
+  if (std::getenv("SPMM_DEBUG"))
+    std::fprintf(stderr, "[spmm] tcgen05 bR=%d nt=%d stages=%d smem=%zu tmem=%d per_sm=%d grid=%lld items=%d panel3d=%d\n",
+                 A.bR, nt, e->stages, e->smem, e->tmem_cols, per_sm, grid, p.n_items, panel3d);
+  e->fn<<<(unsigned)grid, 256, e->smem, r.stream>>>(tmA, tmAlo, tmB, tmBlo, p);
   SPMM_CUDA_TRY(cudaGetLastError());
   return SPMM_OK;
 }
