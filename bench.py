@@ -296,8 +296,9 @@ def run_ours(args, world, rank, local):
         return e0.elapsed_time(e1) / steps
 
     # autotune every precision over the instantiated kernel configurations
-    cands = [m.Config(kernel=k, n_tile=nt, stages=st) for k, nt, st in
-             [(2, 128, 0), (2, 256, 0), (2, 512, 0), (1, 128, 4), (1, 128, 8), (1, 64, 4), (1, 256, 4)]]
+    cands = [m.Config(kernel=k, n_tile=nt, stages=st, acc_buffers=acc, schedule=sch) for k, nt, st, acc, sch in
+             [(2, 256, 4, 2, 0), (2, 256, 4, 2, 1), (2, 256, 2, 2, 0), (2, 512, 3, 1, 0), (2, 512, 3, 2, 0),
+              (2, 128, 4, 2, 0), (1, 128, 8, 0, 0), (1, 128, 4, 0, 0), (1, 64, 4, 0, 0)]]
     results = {}
     prepared = {}
     sampler = ClockSampler(local)
@@ -314,7 +315,7 @@ def run_ours(args, world, rank, local):
             except m.SpmmError:
                 continue
             t = time_loop(probs, cfg, 30)
-            sys.stderr.write("tune %s kernel=%d n_tile=%d stages=%d: %.2f us\n" % (name, cfg.kernel, cfg.n_tile, cfg.stages, t * 1e3))
+            sys.stderr.write("tune %s kernel=%d n_tile=%d stages=%d acc=%d schedule=%d: %.2f us\n" % (name, cfg.kernel, cfg.n_tile, cfg.stages, cfg.acc_buffers, cfg.schedule, t * 1e3))
             if best is None or t < best[0]:
                 best = (t, cfg)
         results[name] = {"ms": best[0], "cfg": best[1], "tflops": flops / best[0] / 1e9,
@@ -409,7 +410,8 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": tuned, "data": "synthetic (seeded generators)",
             "config": {"workload": WORKLOAD, "precision": tuned,
-                       "kernel_config": {"kernel": cfg.kernel, "n_tile": cfg.n_tile, "stages": cfg.stages},
+                       "kernel_config": {"kernel": cfg.kernel, "n_tile": cfg.n_tile, "stages": cfg.stages,
+                                         "acc_buffers": cfg.acc_buffers, "schedule": cfg.schedule},
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
                        "nnzb": nnzb},
@@ -447,7 +449,7 @@ def run_profile(args):
     Bq, Blo, Bs = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), dt)
     A = m.BCSR(M, K, BR, 16, torch.from_numpy(rp).to(dev), torch.from_numpy(ci).to(dev), qv, dt, qlo, qs)
     C = torch.empty((M, N), dtype=torch.float32, device=dev)
-    cfg = m.Config(kernel=args.kernel, n_tile=args.n_tile, stages=args.stages)
+    cfg = m.Config(kernel=args.kernel, n_tile=args.n_tile, stages=args.stages, acc_buffers=args.acc)
     for _ in range(args.launches):
         m.spmm(A, Bq.view(K, N), N=N, C=C, cfg=cfg, B_lo=Blo.view(K, N) if Blo is not None else None,
                b_scale=float(Bs[0]) if Bs is not None else 1.0)
@@ -463,6 +465,7 @@ def main():
     ap.add_argument("--kernel", type=int, default=0)
     ap.add_argument("--n-tile", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)
+    ap.add_argument("--acc", type=int, default=0)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)

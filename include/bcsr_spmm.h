@@ -49,6 +49,8 @@ typedef struct spmm_config {
   int n_tile;    /* output columns per CTA tile: 64, 128 or 256 (0 = auto)           */
   int stages;    /* pipeline depth 2..8 (0 = auto)                                   */
   int ctas_per_sm; /* persistent grid = SMs x this (0 = auto)                          */
+  int acc_buffers; /* tcgen05: TMEM accumulators per CTA, 1 or 2 (0 = auto)          */
+  int schedule;    /* tcgen05: 0 = static item stride, 1 = atomic work queue         */
 } spmm_config;
 
 /* Describes A. All arrays are device pointers. */

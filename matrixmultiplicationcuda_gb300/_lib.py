@@ -30,7 +30,8 @@ class DType(enum.IntEnum):
 
 
 class Config(ctypes.Structure):
-    _fields_ = [("kernel", c_int), ("n_tile", c_int), ("stages", c_int), ("ctas_per_sm", c_int)]
+    _fields_ = [("kernel", c_int), ("n_tile", c_int), ("stages", c_int), ("ctas_per_sm", c_int),
+                ("acc_buffers", c_int), ("schedule", c_int)]
 
 
 class BcsrDesc(ctypes.Structure):

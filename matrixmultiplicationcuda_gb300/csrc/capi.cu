@@ -61,6 +61,26 @@ unsigned* device_error_word() {
   return g_err_word[d];
 }
 
+namespace {
+constexpr int kQueueSlots = 256;
+unsigned* g_queue_pool[kMaxDevices] = {nullptr};
+unsigned g_queue_next[kMaxDevices] = {0};
+}  // namespace
+
+unsigned* work_queue_slot() {
+  int d = current_device();
+  if (d < 0 || d >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_queue_pool[d]) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, kQueueSlots * 2 * sizeof(unsigned)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, kQueueSlots * 2 * sizeof(unsigned)) != cudaSuccess) return nullptr;
+    g_queue_pool[d] = static_cast<unsigned*>(p);
+  }
+  const unsigned i = g_queue_next[d]++ % kQueueSlots;
+  return g_queue_pool[d] + 2 * i;
+}
+
 unsigned long long wait_limit_ns() {
   static unsigned long long v = [] {
     const char* s = std::getenv("SPMM_WAIT_LIMIT_NS");

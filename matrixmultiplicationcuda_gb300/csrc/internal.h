@@ -19,6 +19,10 @@ spmm_status cuda_fail(cudaError_t e, const char* what);
 
 int sm_count();                                  // SMs of the current device
 unsigned* device_error_word();                   // per-device error word (lazy)
+// A zeroed pair {next item, CTAs done} for one persistent launch's work queue.
+// Slots rotate over a per-device pool; each launch's last CTA zeroes its slot
+// again, so a slot is reusable as soon as the launch that used it has ended.
+unsigned* work_queue_slot();
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point.
 spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const void* base,

@@ -50,9 +50,19 @@ struct TcParams {
   unsigned long long timeout_ns;
   unsigned* err;
   int panel3d;      // B panel loaded by one 3-D copy (N % 64 == 0)
+  unsigned* queue;  // [0] next item, [1] CTAs done; NULL = static item striding
 };
 
-template <int BR, int NT, int STAGES, int MODE>
+// BR: block height (the UMMA N); NT: output columns per item; STAGES: ring
+// depth in groups; ACC: TMEM accumulators per CTA (2 = one item's epilogue
+// overlaps the next item's MMAs inside the CTA; 1 = half the TMEM, so two CTAs
+// share an SM and overlap each other instead); G: blocks per group. A group is
+// up to G consecutive stored blocks of one block row: one ring slot holds
+// their A blocks (one TMA copy for a full group, the blocks are contiguous) and
+// their G B panels, and one mbarrier pair tracks it. (An mbarrier wait in the
+// thread that issues UMMAs costs ~200 cycles once UMMAs are in flight, so the
+// MMA thread waits and commits once per group, not once per block.)
+template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
 struct TcCfg {
   static constexpr bool kSplit = MODE == MODE_SPLIT;
   static constexpr int kParts = kSplit ? 2 : 1;
@@ -60,15 +70,15 @@ struct TcCfg {
   static constexpr int kBoxBytes = 16 * 128;          // 16 rows x 64 fp16 columns
   static constexpr int kPanelBytes = (NT / 64) * kBoxBytes;
   static constexpr int kABytes = BR * 32;             // bR rows x 16 fp16
-  static constexpr int kABytesPad = kABytes < 1024 ? 1024 : kABytes;
-  static constexpr int kStageB = kPanelBytes * kParts;
-  static constexpr int kStageA = kABytesPad * kParts;
-  static constexpr int kTx = kPanelBytes * kParts + kABytes * kParts;
+  static constexpr int kAPart = G * kABytes;          // one part (hi or lo) of a group's A blocks
+  static constexpr int kAStage = ((kAPart * kParts + 1023) / 1024) * 1024;
+  static constexpr int kStage = kAStage + G * kPanelBytes * kParts;
   static constexpr int kAccCols = kJ * BR;            // TMEM columns of one accumulator
-  static constexpr int kTmemCols = (2 * kAccCols) < 32 ? 32 : 2 * kAccCols;
-  static constexpr size_t kSmem = 1024 + (size_t)STAGES * (kStageB + kStageA) + 512;
+  static constexpr int kTmemCols = (ACC * kAccCols) < 32 ? 32 : ACC * kAccCols;
+  static constexpr size_t kSmem = 1024 + (size_t)STAGES * kStage + 1024;
   static_assert((kTmemCols & (kTmemCols - 1)) == 0 && kTmemCols <= 512, "TMEM columns");
   static_assert(NT % 128 == 0, "NT");
+  static_assert(G * BR <= 256 && 32 % G == 0, "a group is one TMA box and never straddles an index chunk");
   // kind::f16 instruction descriptor: D f32, A/B f16 or bf16, A MN-major, B K-major,
   // N = BR, M = 128.
   static constexpr uint32_t kIdesc = (1u << 4) | ((MODE == MODE_BF16 ? 1u : 0u) << 7) |
@@ -117,36 +127,44 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-template <int BR, int NT, int STAGES, int MODE>
-__global__ void __launch_bounds__(256, 2)
-    k_bcsr_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
+constexpr int kTcThreads = 320;   // 10 warps
+
+template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
+__global__ void __launch_bounds__(kTcThreads, 2)
+    k_bcsr_tc(const __grid_constant__ CUtensorMap tmA1, const __grid_constant__ CUtensorMap tmAg,
+              const __grid_constant__ CUtensorMap tmAlo1, const __grid_constant__ CUtensorMap tmAlog,
               const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
               const TcParams p) {
-  using Cfg = TcCfg<BR, NT, STAGES, MODE>;
+  using Cfg = TcCfg<BR, NT, STAGES, MODE, ACC, G>;
+  constexpr int kQ = 4;                       // item hand-off ring depth
+  constexpr int kBIssuers = 4;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
-  uint8_t* sB = smem;
-  uint8_t* sA = smem + (size_t)STAGES * Cfg::kStageB;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sA + (size_t)STAGES * Cfg::kStageA);
-  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done; then the TMEM
-  // address and the producer's column-index staging buffer
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)STAGES * Cfg::kStage);
+  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done, qfull[kQ], qempty[kQ];
+  // then the TMEM address and the item ring
   const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES;
   const uint32_t tfull0 = empty0 + 8 * STAGES, tempty0 = tfull0 + 16, done_bar = tempty0 + 16;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
-  int* s_cols = reinterpret_cast<int*>(tmem_slot + 1);    // 32 entries
+  const uint32_t qfull0 = done_bar + 8, qempty0 = qfull0 + 8 * kQ;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5 + 2 * kQ);
+  int* s_item = reinterpret_cast<int*>(tmem_slot + 1);      // kQ x {item, start, end}
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 32) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+      mbar_init(full0 + 8 * s, 1);            // the lead's arrive (it expects the whole group's bytes)
+      mbar_init(empty0 + 8 * s, 1);           // the MMA thread's commit
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(tfull0 + 8 * b, 1);
       mbar_init(tempty0 + 8 * b, 4);
     }
     mbar_init(done_bar, 1);
+    for (int q = 0; q < kQ; ++q) {
+      mbar_init(qfull0 + 8 * q, 1);
+      mbar_init(qempty0 + 8 * q, 1 + kBIssuers + 4);   // MMA, B issuers, epilogue warps
+    }
     fence_mbar_init();
   }
   if (warp == 2) {
@@ -161,146 +179,227 @@ __global__ void __launch_bounds__(256, 2)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    // ------------------------------ TMA producer ---------------------------------
-    // Lane 0 issues every copy; the other lanes fetch column indices 32 at a time
-    // into s_cols and prefetch the next item's row range, so the issuing lane
-    // never waits on a global load or a shuffle between two blocks.
-    if (lane == 0) {
-      tma_prefetch_desc(&tmA);
-      tma_prefetch_desc(&tmB);
+  // Ring entry `it` of the item stream (bounded wait); *item < 0 ends the stream.
+  auto read_item = [&](uint32_t it, int* item, int* start, int* end, unsigned code) -> bool {
+    const uint32_t q = it % kQ;
+    if (!mbar_wait(qfull0 + 8 * q, (it / kQ) & 1, p.timeout_ns)) {
+      atomicOr(p.err, code);
+      return false;
     }
+    *item = s_item[3 * q];
+    *start = s_item[3 * q + 1];
+    *end = s_item[3 * q + 2];
+    mbar_arrive(qempty0 + 8 * q);
+    return true;
+  };
+  const int bidx = warp == 2 ? 0 : warp == 3 ? 1 : warp == 8 ? 2 : warp == 9 ? 3 : -1;
+
+  if (warp == 0) {
+    // ------------------------------ lead producer ----------------------------------
+    // Takes items (work queue or static stride), publishes them through the item
+    // ring (-1 ends the stream), and for each group of the item's blocks claims
+    // the ring slot, expects the group's bytes on its full barrier and copies the
+    // A blocks. The B issuers copy the group's B panels into the same slot.
+    if (lane == 0) {
+      tma_prefetch_desc(&tmAg);
+      tma_prefetch_desc(&tmA1);
+      const uint64_t pol_a = l2_policy_evict_first();
+      auto next_item = [&](int cur) -> int {
+        int v = p.queue ? (int)atomicAdd(p.queue, 1u) : (cur < 0 ? (int)blockIdx.x : cur + (int)gridDim.x);
+        return v < p.n_items ? v : -1;
+      };
+      uint32_t gs = 0, it = 0;
+      bool failed = false;
+      int item = next_item(-1);
+      int start = 0, end = 0;
+      if (item >= 0) {
+        start = __ldg(p.row_ptr + item / p.ntiles);
+        end = __ldg(p.row_ptr + item / p.ntiles + 1);
+      }
+      for (;; ++it) {
+        const uint32_t q = it % kQ;
+        if (it >= (uint32_t)kQ && !mbar_wait(qempty0 + 8 * q, ((it / kQ) + 1) & 1, p.timeout_ns)) {
+          atomicOr(p.err, 4u);
+          failed = true;
+        }
+        s_item[3 * q] = failed ? -1 : item;
+        s_item[3 * q + 1] = start;
+        s_item[3 * q + 2] = end;
+        mbar_arrive(qfull0 + 8 * q);
+        if (item < 0 || failed) break;
+        const int nitem = next_item(item);
+        int nstart = 0, nend = 0;
+        if (nitem >= 0) {
+          nstart = __ldg(p.row_ptr + nitem / p.ntiles);
+          nend = __ldg(p.row_ptr + nitem / p.ntiles + 1);
+        }
+        for (int j0 = start; j0 < end; j0 += G, ++gs) {
+          const int n = min(G, end - j0);
+          const int s = (int)(gs % STAGES);
+          if (gs >= (uint32_t)STAGES && !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
+            atomicOr(p.err, 4u);
+            failed = true;
+            break;
+          }
+          const uint32_t fb = full0 + 8 * s;
+          mbar_arrive_expect_tx(fb, (uint32_t)(n * (Cfg::kABytes + Cfg::kPanelBytes) * Cfg::kParts));
+          uint8_t* a_dst = smem + (size_t)s * Cfg::kStage;
+          const int y0 = j0 * BR;
+          if (n == G) {
+            tma_tile_2d_g2s(smem_u32(a_dst), &tmAg, 0, y0, fb, pol_a);
+            if (Cfg::kSplit) tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kAPart), &tmAlog, 0, y0, fb, pol_a);
+          } else {
+            for (int b = 0; b < n; ++b) {
+              tma_tile_2d_g2s(smem_u32(a_dst + b * Cfg::kABytes), &tmA1, 0, y0 + b * BR, fb, pol_a);
+              if (Cfg::kSplit)
+                tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kAPart + b * Cfg::kABytes), &tmAlo1, 0, y0 + b * BR,
+                                fb, pol_a);
+            }
+          }
+        }
+        if (failed) break;
+        item = nitem;
+        start = nstart;
+        end = nend;
+      }
+      // the last CTA to finish resets the queue for the next launch
+      if (p.queue) {
+        __threadfence();
+        if (atomicAdd(p.queue + 1, 1u) == gridDim.x - 1) {
+          p.queue[0] = 0;
+          p.queue[1] = 0;
+          __threadfence();
+        }
+      }
+    }
+    __syncwarp();
+  } else if (bidx >= 0) {
+    // ------------------------------ B-panel issuers ----------------------------------
+    // Issuer k copies the B panel of block b of each group with b % 4 == k into
+    // the group's slot (a TMA copy holds its issuing thread for ~200 ns, so four
+    // threads share the panels). Its lanes stage column indices 32 at a time,
+    // prefetching the next chunk while lane 0 issues.
+    if (lane == 0) tma_prefetch_desc(&tmB);
     const uint64_t pol_b = l2_policy_evict_last();
-    const uint64_t pol_a = l2_policy_evict_first();
-    uint32_t g = 0;
+    uint32_t gs = 0;
     int failed = 0;
-    int item = blockIdx.x;
-    int br = item / p.ntiles;
-    int start = item < p.n_items ? __ldg(p.row_ptr + br) : 0;
-    int end = item < p.n_items ? __ldg(p.row_ptr + br + 1) : 0;
-    int mycol = (item < p.n_items && lane < end - start) ? __ldg(p.col_idx + start + lane) : 0;
-    for (; item < p.n_items && !failed; item += gridDim.x) {
-      const int nt = item - br * p.ntiles;
-      // next item's row range, loaded now and used after this item's copies
-      const int nitem = item + gridDim.x;
-      const int nbr = nitem / p.ntiles;
-      const int nstart = nitem < p.n_items ? __ldg(p.row_ptr + nbr) : 0;
-      const int nend = nitem < p.n_items ? __ldg(p.row_ptr + nbr + 1) : 0;
+    for (uint32_t it = 0; !failed; ++it) {
+      int item = -1, start = 0, end = 0, ok = 1;
+      if (lane == 0) ok = read_item(it, &item, &start, &end, 4u) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      item = __shfl_sync(0xffffffffu, item, 0);
+      start = __shfl_sync(0xffffffffu, start, 0);
+      end = __shfl_sync(0xffffffffu, end, 0);
+      if (!ok || item < 0) break;
+      const int nt = item - (item / p.ntiles) * p.ntiles;
+      int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
-        s_cols[lane] = mycol;
-        __syncwarp();
-        // column indices of the next chunk (this item's, else the next item's first)
-        const bool more = base + 32 < end;
-        const int nb = more ? base + 32 : nstart;
-        const int nn = more ? end : nend;
-        mycol = (lane < nn - nb && (more || nitem < p.n_items)) ? __ldg(p.col_idx + nb + lane) : 0;
-        if (lane == 0) {
-          for (int i = 0; i < cnt; ++i, ++g) {
-            const int s = (int)(g % STAGES);
-            if (g >= (uint32_t)STAGES && !mbar_wait(empty0 + 8 * s, ((g / STAGES) + 1) & 1, p.timeout_ns)) {
-              atomicOr(p.err, 4u);
-              failed = 1;
-              break;
-            }
-            const int col = s_cols[i];
-            const uint32_t fb = full0 + 8 * s;
-            mbar_arrive_expect_tx(fb, Cfg::kTx);
-            uint8_t* a_dst = sA + (size_t)s * Cfg::kStageA;
-            tma_tile_2d_g2s(smem_u32(a_dst), &tmA, 0, (base + i) * BR, fb, pol_a);
-            if (Cfg::kSplit)
-              tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kABytesPad), &tmAlo, 0, (base + i) * BR, fb, pol_a);
-            uint8_t* b_dst = sB + (size_t)s * Cfg::kStageB;
-            if (p.panel3d) {
-              tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, col * 16, nt * (NT / 64), fb, pol_b);
-              if (Cfg::kSplit)
-                tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, col * 16, nt * (NT / 64), fb, pol_b);
-            } else {
-#pragma unroll
-              for (int b = 0; b < NT / 64; ++b) {
-                tma_tile_2d_g2s(smem_u32(b_dst + b * Cfg::kBoxBytes), &tmB, nt * NT + b * 64, col * 16, fb, pol_b);
+        const int cur = mycol;
+        if (base + 32 < end) mycol = lane < end - base - 32 ? __ldg(p.col_idx + base + 32 + lane) : 0;
+        for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
+          const int n = min(G, cnt - i0);
+          const int s = (int)(gs % STAGES);
+          // every issuer claims the slot through the same empty barrier
+          int bad = 0;
+          if (lane == 0 && gs >= (uint32_t)STAGES &&
+              !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
+            atomicOr(p.err, 4u);
+            bad = 1;
+          }
+          failed = __shfl_sync(0xffffffffu, bad, 0);
+          if (failed) break;
+          uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
+          for (int b = bidx; b < n; b += kBIssuers) {
+            const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
+            if (lane == 0) {
+              const uint32_t fb = full0 + 8 * s;
+              uint8_t* b_dst = b_dst0 + (size_t)b * Cfg::kPanelBytes * Cfg::kParts;
+              if (p.panel3d) {
+                tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, col * 16, nt * (NT / 64), fb, pol_b);
                 if (Cfg::kSplit)
-                  tma_tile_2d_g2s(smem_u32(b_dst + Cfg::kPanelBytes + b * Cfg::kBoxBytes), &tmBlo,
-                                  nt * NT + b * 64, col * 16, fb, pol_b);
+                  tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, col * 16, nt * (NT / 64), fb, pol_b);
+              } else {
+#pragma unroll
+                for (int bx = 0; bx < NT / 64; ++bx) {
+                  tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), &tmB, nt * NT + bx * 64, col * 16, fb, pol_b);
+                  if (Cfg::kSplit)
+                    tma_tile_2d_g2s(smem_u32(b_dst + Cfg::kPanelBytes + bx * Cfg::kBoxBytes), &tmBlo,
+                                    nt * NT + bx * 64, col * 16, fb, pol_b);
+                }
               }
             }
           }
         }
-        failed = __shfl_sync(0xffffffffu, failed, 0);
-        __syncwarp();
       }
-      if (start >= end) {
-        // empty row: the prefetch above did not run; fetch the next item's first chunk
-        mycol = (nitem < p.n_items && lane < nend - nstart) ? __ldg(p.col_idx + nstart + lane) : 0;
-      }
-      br = nbr;
-      start = nstart;
-      end = nend;
     }
   } else if (warp == 1) {
     // ------------------------------ MMA issuer -----------------------------------
     if (lane == 0) {
-      uint32_t g = 0, it = 0;
+      uint32_t gs = 0, it = 0;
       bool failed = false;
-      int item = blockIdx.x;
-      int start = item < p.n_items ? __ldg(p.row_ptr + item / p.ntiles) : 0;
-      int end = item < p.n_items ? __ldg(p.row_ptr + item / p.ntiles + 1) : 0;
-      for (; item < p.n_items && !failed; item += gridDim.x, ++it) {
-        const int nitem = item + gridDim.x;
-        const int nstart = nitem < p.n_items ? __ldg(p.row_ptr + nitem / p.ntiles) : 0;
-        const int nend = nitem < p.n_items ? __ldg(p.row_ptr + nitem / p.ntiles + 1) : 0;
-        const uint32_t acc = it & 1;
-        if (it >= 2 && !mbar_wait(tempty0 + 8 * acc, ((it >> 1) + 1) & 1, p.timeout_ns)) {
+      for (;; ++it) {
+        int item, start, end;
+        if (!read_item(it, &item, &start, &end, 8u) || item < 0) break;
+        const uint32_t acc = it % ACC;
+        if (it >= (uint32_t)ACC && !mbar_wait(tempty0 + 8 * acc, ((it / ACC) + 1) & 1, p.timeout_ns)) {
           atomicOr(p.err, 8u);
           break;
         }
         tc_fence_after();
         const uint32_t d0 = tmem + acc * Cfg::kAccCols;
-        for (int k = start; k < end; ++k, ++g) {
-          const int s = (int)(g % STAGES);
-          if (!mbar_wait(full0 + 8 * s, (g / STAGES) & 1, p.timeout_ns)) {
+        for (int j0 = start; j0 < end; j0 += G, ++gs) {
+          const int n = min(G, end - j0);
+          const int s = (int)(gs % STAGES);
+          if (!mbar_wait(full0 + 8 * s, (gs / STAGES) & 1, p.timeout_ns)) {
             atomicOr(p.err, 8u);
             failed = true;
             break;
           }
           tc_fence_after();
-          const uint32_t a_addr = smem_u32(sA + (size_t)s * Cfg::kStageA);
-          const uint32_t b_addr = smem_u32(sB + (size_t)s * Cfg::kStageB);
-          const uint64_t blk_hi = smem_desc(a_addr, 16, 256, kLayoutSW32);
-          const uint32_t accum = (k != start) ? 1u : 0u;
+          const uint32_t a_slot = smem_u32(smem + (size_t)s * Cfg::kStage);
+          const uint32_t b_slot = a_slot + Cfg::kAStage;
+          for (int b = 0; b < n; ++b) {
+            const uint32_t b_addr = b_slot + b * Cfg::kPanelBytes * Cfg::kParts;
+            const uint64_t blk_hi = smem_desc(a_slot + b * Cfg::kABytes, 16, 256, kLayoutSW32);
+            const uint32_t accum = (j0 + b != start) ? 1u : 0u;
 #pragma unroll
-          for (int j = 0; j < Cfg::kJ; ++j) {
-            const uint64_t pan_hi = smem_desc(b_addr + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
-            umma_f16(d0 + j * BR, pan_hi, blk_hi, Cfg::kIdesc, accum);
-            if constexpr (Cfg::kSplit) {
-              const uint64_t pan_lo =
-                  smem_desc(b_addr + Cfg::kPanelBytes + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
-              const uint64_t blk_lo = smem_desc(a_addr + Cfg::kABytesPad, 16, 256, kLayoutSW32);
-              umma_f16(d0 + j * BR, pan_lo, blk_hi, Cfg::kIdesc, 1u);
-              umma_f16(d0 + j * BR, pan_hi, blk_lo, Cfg::kIdesc, 1u);
+            for (int j = 0; j < Cfg::kJ; ++j) {
+              const uint64_t pan_hi = smem_desc(b_addr + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
+              umma_f16(d0 + j * BR, pan_hi, blk_hi, Cfg::kIdesc, accum);
+              if constexpr (Cfg::kSplit) {
+                const uint64_t pan_lo =
+                    smem_desc(b_addr + Cfg::kPanelBytes + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
+                const uint64_t blk_lo =
+                    smem_desc(a_slot + Cfg::kAPart + b * Cfg::kABytes, 16, 256, kLayoutSW32);
+                umma_f16(d0 + j * BR, pan_lo, blk_hi, Cfg::kIdesc, 1u);
+                umma_f16(d0 + j * BR, pan_hi, blk_lo, Cfg::kIdesc, 1u);
+              }
             }
           }
-          umma_commit(empty0 + 8 * s);   // frees the ring slot once these MMAs have read it
+          umma_commit(empty0 + 8 * s);   // frees the group's slot once these MMAs have read it
         }
         if (failed) break;
         umma_commit(tfull0 + 8 * acc);   // accumulator ready (immediately, for an empty row)
-        start = nstart;
-        end = nend;
       }
       // every MMA this thread issued has completed before TMEM is released
       umma_commit(done_bar);
       if (!mbar_wait(done_bar, 0, p.timeout_ns)) atomicOr(p.err, 8u);
     }
     __syncwarp();
-  } else if (warp >= 4) {
+  } else if (warp >= 4 && warp < 8) {
     // ------------------------------ epilogue (warps 4-7) ---------------------------
-    const int q = warp & 3;                 // TMEM lane quarter this warp may access
-    uint32_t it = 0;
-    for (int item = blockIdx.x; item < p.n_items; item += gridDim.x, ++it) {
+    const int q4 = warp & 3;                // TMEM lane quarter this warp may access
+    for (uint32_t it = 0;; ++it) {
+      int item = -1, start = 0, end = 0, ok = 1;
+      if (lane == 0) ok = read_item(it, &item, &start, &end, 16u) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      item = __shfl_sync(0xffffffffu, item, 0);
+      const bool empty = __shfl_sync(0xffffffffu, start == end ? 1 : 0, 0) != 0;
+      if (!ok || item < 0) break;
       const int br = item / p.ntiles, nt = item - br * p.ntiles;
-      const bool empty = __ldg(p.row_ptr + br) == __ldg(p.row_ptr + br + 1);
-      const uint32_t acc = it & 1;
-      if (!mbar_wait(tfull0 + 8 * acc, (it >> 1) & 1, p.timeout_ns)) {
+      const uint32_t acc = it % ACC;
+      if (!mbar_wait(tfull0 + 8 * acc, (it / ACC) & 1, p.timeout_ns)) {
         if (lane == 0) atomicOr(p.err, 16u);
         break;
       }
@@ -308,9 +407,9 @@ __global__ void __launch_bounds__(256, 2)
       const long long row0 = (long long)br * BR;
 #pragma unroll 1
       for (int j = 0; j < Cfg::kJ; ++j) {
-        const int n = nt * NT + j * 128 + q * 32 + lane;
+        const int n = nt * NT + j * 128 + q4 * 32 + lane;
         float* cptr = p.C + row0 * p.ldc + n;
-        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + acc * Cfg::kAccCols + j * BR;
+        const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + acc * Cfg::kAccCols + j * BR;
 #pragma unroll
         for (int c0 = 0; c0 < BR; c0 += 16) {
           float v[16];
@@ -342,25 +441,33 @@ __global__ void __launch_bounds__(256, 2)
 }
 
 using TcFn = void (*)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap,
-                      const TcParams);
+                      const CUtensorMap, const CUtensorMap, const TcParams);
 struct TcEntry {
-  int br, mode, nt, stages;
+  int br, mode, nt, stages, acc, group;
   TcFn fn;
   size_t smem;
   int tmem_cols;
 };
-#define SPMM_TC_ENTRY(BR, NT, ST, MODE) \
-  TcEntry{BR, MODE, NT, ST, &k_bcsr_tc<BR, NT, ST, MODE>, TcCfg<BR, NT, ST, MODE>::kSmem, TcCfg<BR, NT, ST, MODE>::kTmemCols}
+#define SPMM_TC_ENTRY(BR, NT, ST, MODE, ACC, G)                                            \
+  TcEntry{BR, MODE, NT, ST, ACC, G, &k_bcsr_tc<BR, NT, ST, MODE, ACC, G>,                  \
+          TcCfg<BR, NT, ST, MODE, ACC, G>::kSmem, TcCfg<BR, NT, ST, MODE, ACC, G>::kTmemCols}
+
+// Instantiated (block height, column tile, ring depth in groups, accumulators,
+// group size) per type.
+// The first entry of a (block height, column tile) pair is its default.
+#define SPMM_TC_SHAPES(MODE)                                                                         \
+  SPMM_TC_ENTRY(64, 256, 4, MODE, 2, 2), SPMM_TC_ENTRY(64, 256, 2, MODE, 2, 4),                     \
+      SPMM_TC_ENTRY(64, 512, 3, MODE, 1, 2), SPMM_TC_ENTRY(64, 512, 3, MODE, 2, 4),                 \
+      SPMM_TC_ENTRY(64, 128, 4, MODE, 2, 4), SPMM_TC_ENTRY(32, 256, 3, MODE, 2, 4),                 \
+      SPMM_TC_ENTRY(32, 512, 3, MODE, 1, 2), SPMM_TC_ENTRY(16, 256, 3, MODE, 2, 4),                 \
+      SPMM_TC_ENTRY(16, 512, 3, MODE, 1, 2)
 
 const TcEntry kTcEntries[] = {
-    SPMM_TC_ENTRY(64, 128, 8, MODE_F16),   SPMM_TC_ENTRY(64, 256, 6, MODE_F16),
-    SPMM_TC_ENTRY(64, 512, 6, MODE_F16),   SPMM_TC_ENTRY(32, 256, 8, MODE_F16),
-    SPMM_TC_ENTRY(64, 128, 16, MODE_F16),  SPMM_TC_ENTRY(64, 256, 10, MODE_F16),
-    SPMM_TC_ENTRY(64, 256, 4, MODE_F16),   SPMM_TC_ENTRY(64, 512, 10, MODE_F16),
-    SPMM_TC_ENTRY(16, 256, 8, MODE_F16),   SPMM_TC_ENTRY(64, 128, 8, MODE_BF16),
-    SPMM_TC_ENTRY(64, 256, 6, MODE_BF16),  SPMM_TC_ENTRY(64, 512, 6, MODE_BF16),
-    SPMM_TC_ENTRY(32, 256, 8, MODE_BF16),  SPMM_TC_ENTRY(16, 256, 8, MODE_BF16),
-    SPMM_TC_ENTRY(64, 256, 4, MODE_SPLIT), SPMM_TC_ENTRY(64, 128, 6, MODE_SPLIT),
+    SPMM_TC_SHAPES(MODE_F16),
+    SPMM_TC_SHAPES(MODE_BF16),
+    SPMM_TC_ENTRY(64, 256, 2, MODE_SPLIT, 2, 2),
+    SPMM_TC_ENTRY(64, 128, 3, MODE_SPLIT, 2, 2),
+    SPMM_TC_ENTRY(64, 512, 2, MODE_SPLIT, 1, 1),
 };
 
 }  // namespace
@@ -372,28 +479,37 @@ spmm_status launch_tc(const LaunchRequest& r) {
                                                : A.dtype == SPMM_F16_SPLIT ? MODE_SPLIT : -1;
   if (mode < 0) return fail(SPMM_ERR_UNSUPPORTED, "tcgen05 pipeline: fp16, bf16 and split fp16 only");
   int nt = r.cfg.n_tile;
-  if (nt <= 0) nt = r.N >= 512 && A.bR == 64 && mode != MODE_SPLIT ? 256 : (r.N >= 256 ? 256 : 128);
+  if (nt <= 0) nt = (r.N <= 128 && A.bR == 64) ? 128 : 256;
+  if (nt < 256 && A.bR != 64) nt = 256;
+  const int acc = r.cfg.acc_buffers;
   const TcEntry* e = nullptr;
-  for (const TcEntry& c : kTcEntries)
-    if (c.br == A.bR && c.mode == mode && c.nt == nt && (r.cfg.stages <= 0 || c.stages == r.cfg.stages)) {
-      e = &c;
-      break;
-    }
+  for (const TcEntry& c : kTcEntries) {
+    if (c.br != A.bR || c.mode != mode || c.nt != nt) continue;
+    if (r.cfg.stages > 0 && c.stages != r.cfg.stages) continue;
+    if (acc > 0 && c.acc != acc) continue;
+    e = &c;
+    break;
+  }
   if (!e)
     return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for bR=" + std::to_string(A.bR) +
                                           " n_tile=" + std::to_string(nt));
   // A's values viewed as a [rows x 16] fp16 tensor; rows bounded by the densest
-  // possible matrix (only coordinates of stored blocks are ever requested).
-  const unsigned long long rows_bound = (unsigned long long)(A.M / A.bR) * (A.K / 16) * A.bR;
+  // possible matrix (only coordinates of stored blocks are ever requested: a
+  // group copy is issued only for kGroup consecutive blocks of one block row).
+  const unsigned long long rows_bound =
+      std::max<unsigned long long>((unsigned long long)(A.M / A.bR) * (A.K / 16) * A.bR, 256ull);
   if (rows_bound >= (1ull << 31)) return fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline");
-  CUtensorMap tmA, tmAlo, tmB, tmBlo;
+  CUtensorMap tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo;
   const void* vals = A.vals ? A.vals : B.data;   // no stored blocks: never dereferenced
-  spmm_status st = encode_tile_map_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals, 16, rows_bound, 32,
-                                      16, (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
+  spmm_status st = encode_tile_map_2d(&tmA1, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals, 16, rows_bound, 32, 16,
+                                      (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
+  if (st != SPMM_OK) return st;
+  st = encode_tile_map_2d(&tmAg, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals, 16, rows_bound, 32, 16,
+                          (uint32_t)(e->group * A.bR), CU_TENSOR_MAP_SWIZZLE_32B);
   if (st != SPMM_OK) return st;
   // B panels: one 3-D copy per panel when N is a multiple of 64, else one 2-D
   // copy per 64-column box.
-  int panel3d = (r.N % 64 == 0 && r.cfg.kernel != 3) ? 1 : 0;
+  int panel3d = (r.N % 64 == 0) ? 1 : 0;
   if (panel3d && encode_panel_map_3d(&tmB, B.data, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * 2,
                                      (uint32_t)(nt / 64)) != SPMM_OK)
     panel3d = 0;
@@ -402,12 +518,16 @@ spmm_status launch_tc(const LaunchRequest& r) {
                             (uint64_t)B.ldb * 2, 64, 16, CU_TENSOR_MAP_SWIZZLE_128B);
     if (st != SPMM_OK) return st;
   }
-  tmAlo = tmA;
+  tmAlo1 = tmA1;
+  tmAlog = tmAg;
   tmBlo = tmB;
   if (mode == MODE_SPLIT) {
     const void* lo = A.vals_lo ? A.vals_lo : B.data_lo;
-    st = encode_tile_map_2d(&tmAlo, CU_TENSOR_MAP_DATA_TYPE_UINT16, lo, 16, rows_bound, 32, 16,
+    st = encode_tile_map_2d(&tmAlo1, CU_TENSOR_MAP_DATA_TYPE_UINT16, lo, 16, rows_bound, 32, 16,
                             (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
+    if (st != SPMM_OK) return st;
+    st = encode_tile_map_2d(&tmAlog, CU_TENSOR_MAP_DATA_TYPE_UINT16, lo, 16, rows_bound, 32, 16,
+                            (uint32_t)(e->group * A.bR), CU_TENSOR_MAP_SWIZZLE_32B);
     if (st != SPMM_OK) return st;
     st = panel3d ? encode_panel_map_3d(&tmBlo, B.data_lo, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * 2,
                                        (uint32_t)(nt / 64))
@@ -426,6 +546,8 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.timeout_ns = wait_limit_ns();
   p.err = device_error_word();
   p.panel3d = panel3d;
+  // items: static stride by default, or a work queue on request
+  p.queue = r.cfg.schedule == 1 ? work_queue_slot() : nullptr;
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
   SPMM_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(e->fn),
@@ -445,9 +567,12 @@ spmm_status launch_tc(const LaunchRequest& r) {
   long long grid = (long long)sm_count() * per_sm;
   if (grid > p.n_items) grid = p.n_items;
   if (std::getenv("SPMM_DEBUG"))
-    std::fprintf(stderr, "[spmm] tcgen05 bR=%d nt=%d stages=%d smem=%zu tmem=%d per_sm=%d grid=%lld items=%d panel3d=%d\n",
-                 A.bR, nt, e->stages, e->smem, e->tmem_cols, per_sm, grid, p.n_items, panel3d);
-  e->fn<<<(unsigned)grid, 256, e->smem, r.stream>>>(tmA, tmAlo, tmB, tmBlo, p);
+    std::fprintf(stderr,
+                 "[spmm] tcgen05 bR=%d nt=%d stages=%d acc=%d group=%d smem=%zu tmem=%d per_sm=%d grid=%lld "
+                 "items=%d panel3d=%d queue=%d\n",
+                 A.bR, nt, e->stages, e->acc, e->group, e->smem, e->tmem_cols, per_sm, grid, p.n_items, panel3d,
+                 p.queue != nullptr);
+  e->fn<<<(unsigned)grid, kTcThreads, e->smem, r.stream>>>(tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo, p);
   SPMM_CUDA_TRY(cudaGetLastError());
   return SPMM_OK;
 }

@@ -5,6 +5,7 @@ rows, partial column tiles and poisoned outputs.
 Bars: fp16 / bf16 inputs rounded first, so the FP64 product of the rounded
 values is the reference and only fp32 accumulation order differs:
 normwise error <= 1e-5. Split fp16 hi+lo against the fp32 values: <= 2e-6.
+Rows of ~50 blocks (K = 4096 at 20 %) accumulate ~800 terms in fp32: <= 3e-5.
 """
 import numpy as np
 import pytest
@@ -15,9 +16,11 @@ from oracle import oracle
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(64, 128, "f16"), (64, 256, "f16"), (64, 512, "f16"), (32, 256, "f16"), (16, 256, "f16"),
-         (64, 128, "bf16"), (64, 256, "bf16"), (64, 512, "bf16"), (32, 256, "bf16"), (16, 256, "bf16"),
-         (64, 256, "split"), (64, 128, "split")]
+CASES = [(64, 128, "f16", 2), (64, 256, "f16", 2), (64, 512, "f16", 1), (64, 512, "f16", 2),
+         (32, 256, "f16", 2), (32, 512, "f16", 1), (16, 256, "f16", 2), (16, 512, "f16", 1),
+         (64, 128, "bf16", 2), (64, 256, "bf16", 2), (64, 512, "bf16", 1), (64, 512, "bf16", 2),
+         (32, 256, "bf16", 2), (16, 512, "bf16", 1),
+         (64, 256, "split", 2), (64, 128, "split", 2), (64, 512, "split", 1)]
 DT = {"f16": m.DType.F16, "bf16": m.DType.BF16, "split": m.DType.F16_SPLIT}
 
 
@@ -30,25 +33,30 @@ def rounded(x, name):
     return x.astype(np.float64)
 
 
-@pytest.mark.parametrize("bR,nt,name", CASES)
-@pytest.mark.parametrize("N", [64, 200, 512])
-def test_tc_matches_fp64(dev, bR, nt, name, N):
+@pytest.mark.parametrize("bR,nt,name,acc", CASES)
+@pytest.mark.parametrize("N,K,dens,queue", [(64, 1024, 0.06, 1), (200, 1024, 0.06, 1), (512, 1024, 0.06, 0),
+                                            (512, 4096, 0.2, 1)])
+def test_tc_matches_fp64(dev, bR, nt, name, acc, N, K, dens, queue):
+    """K = 4096 at 20 % gives rows of ~50 blocks: index chunks of 32 and partial
+    A groups at row ends; queue=1 takes items from the work queue."""
     N = N - N % 8
-    M, K = 512, 1024
-    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, 0.06, 1.5, seed=bR + N)
+    M = 512
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, dens, 1.5, seed=bR + N)
     vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=3)
     Bf = m.gen_dense(K, N, m.DIST_UNIFORM, seed=4)
     A = m.BCSR.from_host(M, K, bR, rp, ci, vals, DT[name], device=dev)
     Bq, Blo, _ = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), DT[name])
     C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
     m.spmm(A, Bq.view(K, N), N=N, C=C, B_lo=Blo.view(K, N) if Blo is not None else None,
-           cfg=m.Config(kernel=2, n_tile=nt))
+           cfg=m.Config(kernel=2, n_tile=nt, acc_buffers=acc, schedule=queue))
     m.device_error_check()
     got = C.cpu().numpy()
     ref = oracle.bcsr_matmul_f64(rp, ci, rounded(vals, name), bR, 16, rounded(Bf, name))
     assert np.isfinite(got).all()
     mx, fr = oracle.rel_errors(got, ref)
-    bar = 2e-6 if name == "split" else 1e-5
+    # fp32 accumulation over ~16 x blocks-per-row terms sets the floor: the
+    # K = 4096, 20 % rows sum ~800 products
+    bar = (2e-6 if name == "split" else 1e-5) if K <= 1024 else 3e-5
     assert mx <= bar and fr <= bar, (mx, fr)
     empty = np.nonzero(np.diff(rp) == 0)[0]
     for br in empty[:4]:
