@@ -178,6 +178,30 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count,
 spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream);
 spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
 
+/* ---- allocation-free variant ---------------------------------------------------
+ * No counterpart in the reference. For callers that cannot call cudaMalloc (a
+ * host application or allocator that owns all device memory, a memory budget
+ * that forbids the CUDA allocator, code that must not allocate while a stream
+ * is being captured): the same product as spmm_bcsr_mm on the tcgen05 pipeline
+ * with its work queue, but its scratch -- the device error word and the
+ * queue's two counters, 12 bytes -- lives in a fixed 256-byte __device__ array
+ * compiled into the library (held on every GPU that loads the library until
+ * the process exits), and the call allocates nothing. The caller still passes
+ * A, B and C.
+ *  - fp16, bf16 and split fp16 only (E4M3 runs on a path with allocated scratch).
+ *  - At most 2^30 work items (block rows x 128-column tiles): the queue
+ *    counters are 32-bit. Larger problems return SPMM_ERR_SCRATCH_TOO_SMALL.
+ *  - The first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - Every call shares the array (one copy per device) and clears it on its
+ *    stream first; calls whose launches overlap on the same GPU (for example on
+ *    two streams) race on it, so serialise them.
+ * spmm_noalloc_error_check synchronises the stream and reports a timed-out
+ * pipeline wait of the last allocation-free call (SPMM_ERR_TIMEOUT). */
+spmm_status spmm_bcsr_mm_noalloc(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N,
+                                 float* C, int ldc, const spmm_config* cfg, void* stream);
+spmm_status spmm_noalloc_error_check(void* stream);
+
 /* ---- diagnostics ---------------------------------------------------------------
  * Runs one block of the pipeline's bounded mbarrier wait on a barrier that no
  * one arrives on, with the given limit in nanoseconds; returns SPMM_ERR_TIMEOUT

@@ -76,6 +76,9 @@ _SIGS = {
     "spmm_batch_run": (c_int, [c_vp, c_vp]),
     "spmm_batch_plan_destroy": (c_int, [c_vp]),
     "spmm_debug_wait_timeout": (c_int, [c_ull, c_vp]),
+    "spmm_bcsr_mm_noalloc": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp,
+                                     c_int, ctypes.POINTER(Config), c_vp]),
+    "spmm_noalloc_error_check": (c_int, [c_vp]),
     # host side (csrc/host)
     "spmm_generate_matrix": (c_int, [c_int, c_int, c_double, c_char_p, c_int, c_uint, c_vp]),
     "spmm_gen_structure": (c_ll, [c_int, c_int, c_int, c_int, c_double, c_double, c_ull, c_vp, c_vp]),

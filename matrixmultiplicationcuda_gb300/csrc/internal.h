@@ -45,6 +45,10 @@ struct LaunchRequest {
   long long ldc;
   spmm_config cfg;
   cudaStream_t stream;
+  // Caller-provided scratch (both NULL for every entry point except the
+  // allocation-free one): the device error word and the work-queue pair.
+  unsigned* err_word = nullptr;
+  unsigned* queue = nullptr;
 };
 // mma.sync family (spmm_mma.cu)
 spmm_status launch_mma(const LaunchRequest& r);

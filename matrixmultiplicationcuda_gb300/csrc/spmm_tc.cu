@@ -544,10 +544,10 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.ntiles = (r.N + nt - 1) / nt;
   p.n_items = (A.M / A.bR) * p.ntiles;
   p.timeout_ns = wait_limit_ns();
-  p.err = device_error_word();
+  p.err = r.err_word ? r.err_word : device_error_word();
   p.panel3d = panel3d;
   // items: static stride by default, or a work queue on request
-  p.queue = r.cfg.schedule == 1 ? work_queue_slot() : nullptr;
+  p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
   SPMM_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(e->fn),
