@@ -36,6 +36,7 @@ from .bcsr import (  # noqa: F401
     quantize,
     device_error_check,
     debug_wait_timeout,
+    BatchPlan,
 )
 from .host import (  # noqa: F401
     generate_matrix,
@@ -54,5 +55,7 @@ from .host import (  # noqa: F401
     DIST_SCALED_NORMAL,
     DIST_NORMAL,
 )
+
+from .workloads import uneven_batch_specs, make_problem  # noqa: F401,E402
 
 __all__ = [n for n in dir() if not n.startswith("_")]

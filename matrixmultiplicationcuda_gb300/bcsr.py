@@ -185,3 +185,44 @@ def device_error_check(stream=None):
 def debug_wait_timeout(timeout_ns, stream=None):
     """Returns the Status of the bounded-wait diagnostic (TIMEOUT expected)."""
     return Status(lib().spmm_debug_wait_timeout(int(timeout_ns), stream_handle(stream)))
+
+
+class BatchPlan:
+    """Many independent products C_i = A_i @ B_i in one persistent launch
+    (spmm_batch_plan_create / spmm_batch_run). The plan reads each A_i's row
+    pointers once, orders the (problem, block row, column tile) items heaviest
+    first and keeps them on the device; run() only launches, so it can be
+    captured in a CUDA graph and replayed. The tensors are referenced by the
+    plan and must stay alive and in place while it is used."""
+
+    def __init__(self, problems, cfg: Optional[Config] = None):
+        """problems: list of (A: BCSR, B [K, N] tensor, C [M, N] fp32 tensor)."""
+        from ._lib import Problem
+        self._keep = list(problems)
+        arr = (Problem * max(len(problems), 1))()
+        for i, (A, B, C) in enumerate(problems):
+            arr[i].A = A.desc()
+            arr[i].B = _dense_desc(B, ldb=B.stride(0))
+            arr[i].N = int(B.shape[1])
+            arr[i].C = C.data_ptr()
+            arr[i].ldc = int(C.stride(0))
+        self._arr = arr
+        h = ctypes.c_void_p()
+        check(lib().spmm_batch_plan_create(arr, len(problems),
+                                           ctypes.byref(cfg) if cfg is not None else None,
+                                           ctypes.byref(h)))
+        self._h = h
+
+    def run(self, stream=None):
+        check(lib().spmm_batch_run(self._h, stream_handle(stream)))
+
+    def close(self):
+        if self._h:
+            lib().spmm_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

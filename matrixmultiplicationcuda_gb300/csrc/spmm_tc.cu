@@ -10,24 +10,25 @@
 // segments of C.
 //
 // Operands come from shared memory through TMA:
-//   * the B row-panel (16 rows x NT columns) as 64-column boxes with 128-byte
-//     swizzle -- the MMA's A operand in the MN-major canonical layout
-//     (atoms of 64 columns x 8 rows; 8-row groups 1024 B apart, 64-column
-//     atoms 2048 B apart);
-//   * the A block (bR rows x 16) as one box with 32-byte swizzle -- the MMA's
-//     B operand in the K-major canonical layout (8-row groups 256 B apart).
+//   * the B row-panel (16 rows x NT columns) as 64-column atoms with 128-byte
+//     swizzle -- the MMA's A operand in the MN-major canonical layout (8-row
+//     groups 1024 B apart, 64-column atoms 2048 B apart); one 3-D copy per
+//     panel when N % 64 == 0;
+//   * the A blocks (bR rows x 16) with 32-byte swizzle -- the MMA's B operand
+//     in the K-major canonical layout (8-row groups 256 B apart); the blocks
+//     of a group are contiguous in memory and arrive in one copy.
 //
-// Warp roles (256 threads, two CTAs per SM): warp 0 streams TMA copies into a
-// STAGES-deep mbarrier ring (one copy for the A block and, when N % 64 == 0,
-// one 3-D copy for the whole B panel: a TMA instruction holds its issuing thread
-// for tens of cycles, so copies per block bound the block rate); warp 1 (one
-// thread) issues the UMMAs, releases each ring slot with tcgen05.commit and
-// hands finished accumulators to the epilogue; warp 2 owns the TMEM
-// allocation; warps 4-7 drain TMEM (double-buffered, so the next item's MMAs
-// overlap) with tcgen05.ld and store C with streaming stores. The grid is persistent over
-// items = (block row, NT-column tile). Every mbarrier wait is bounded; a wait
-// that gives up sets the device error word, all roles leave their loops, and
-// the allocating warp frees TMEM after the MMA thread has drained its commits.
+// Warp roles (10 warps, two CTAs per SM): warp 0 takes items (static stride
+// or work queue), publishes them through an item ring and copies A groups;
+// warps 2, 3, 8, 9 copy the B panels (a TMA instruction holds its issuing
+// thread for ~200 ns, so four threads share them); warp 1 (one thread) issues
+// the UMMAs, releases each group's ring slot with tcgen05.commit and hands
+// finished accumulators to the epilogue; warp 2 owns the TMEM allocation;
+// warps 4-7 drain TMEM (double-buffered, so the next item's MMAs overlap) with
+// tcgen05.ld and store C with streaming stores. Items = (block row, NT-column
+// tile). Every mbarrier wait is bounded; a wait that gives up sets the device
+// error word, all roles leave their loops, and the allocating warp frees TMEM
+// after the MMA thread has drained its commits.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -35,6 +36,7 @@
 #include "internal.h"
 #include "ptx.cuh"
 #include "spmm_mma.cuh"
+#include "tcgen05.cuh"
 
 namespace spmm {
 namespace {
@@ -85,47 +87,6 @@ struct TcCfg {
                                      ((MODE == MODE_BF16 ? 1u : 0u) << 10) | (1u << 15) |
                                      ((uint32_t)(BR >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 };
-
-// Shared-memory matrix descriptor (tcgen05): start, leading / stride byte
-// offsets (16-byte units), version 1, swizzle mode.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo,
-                                              uint32_t layout) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | ((uint64_t)layout << 61);
-}
-constexpr uint32_t kLayoutSW128 = 2, kLayoutSW32 = 6;
-
-__device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-// 16 consecutive TMEM columns of this thread's lane.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 constexpr int kTcThreads = 320;   // 10 warps
 
@@ -300,9 +261,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
           const int n = min(G, cnt - i0);
           const int s = (int)(gs % STAGES);
-          // every issuer claims the slot through the same empty barrier
+          // Wait for the slot only in groups this issuer copies into: such a
+          // group cannot be released without its bytes, so the slot's empty
+          // barrier is at most one phase ahead. (An issuer that also waited in
+          // groups it has no block in could fall two phases behind and miss a
+          // parity flip.)
           int bad = 0;
-          if (lane == 0 && gs >= (uint32_t)STAGES &&
+          if (lane == 0 && bidx < n && gs >= (uint32_t)STAGES &&
               !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
             atomicOr(p.err, 4u);
             bad = 1;

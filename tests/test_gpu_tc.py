@@ -61,3 +61,23 @@ def test_tc_matches_fp64(dev, bR, nt, name, acc, N, K, dens, queue):
     empty = np.nonzero(np.diff(rp) == 0)[0]
     for br in empty[:4]:
         assert np.all(got[br * bR:(br + 1) * bR] == 0)
+
+
+@pytest.mark.parametrize("queue", [0, 1])
+def test_tc_short_rows_repeated(dev, queue):
+    """Rows of zero to two blocks, launched back to back: most groups hold one
+    block, so some B-panel issuers copy nothing for long stretches. Every launch
+    must finish without a timed-out pipeline wait and match the FP64 oracle."""
+    M, K, N, bR = 4096, 2048, 256, 16
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_RANDOM, 0.006, 0.0, seed=77)
+    vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=78)
+    Bf = m.gen_dense(K, N, m.DIST_UNIFORM, seed=79)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, m.DType.F16, device=dev)
+    B = torch.from_numpy(Bf).to(dev).half()
+    C = torch.empty((M, N), dtype=torch.float32, device=dev)
+    for _ in range(40):
+        m.spmm(A, B, N=N, C=C, cfg=m.Config(kernel=2, n_tile=256, acc_buffers=2, schedule=queue))
+    m.device_error_check()
+    ref = oracle.bcsr_matmul_f64(rp, ci, rounded(vals, "f16"), bR, 16, rounded(Bf, "f16"))
+    mx, fr = oracle.rel_errors(C.cpu().numpy(), ref)
+    assert mx <= 1e-5 and fr <= 1e-5, (mx, fr)
