@@ -45,12 +45,16 @@ typedef enum spmm_dtype {
 
 /* Kernel configuration. Zero-initialised = let the library choose. */
 typedef struct spmm_config {
-  int kernel;    /* 0 = auto, 1 = mma.sync pipeline, 2 = tcgen05 pipeline (bR = 64)  */
+  int kernel;    /* 0 = auto, 1 = mma.sync pipeline, 2 = tcgen05 pipeline              */
   int n_tile;    /* output columns per CTA tile: 64, 128 or 256 (0 = auto)           */
   int stages;    /* pipeline depth 2..8 (0 = auto)                                   */
   int ctas_per_sm; /* persistent grid = SMs x this (0 = auto)                          */
   int acc_buffers; /* tcgen05: TMEM accumulators per CTA, 1 or 2 (0 = auto)          */
   int schedule;    /* tcgen05: 0 = static item stride, 1 = atomic work queue         */
+  int split_k;     /* tcgen05: split each block row's blocks over this many work
+                      items whose partial products are added into C (C is
+                      zeroed first; the order of the additions varies from run
+                      to run). 0 or 1 = no split; at most 16.                   */
 } spmm_config;
 
 /* Describes A. All arrays are device pointers. */
@@ -177,6 +181,75 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count,
                                    const spmm_config* cfg, spmm_batch_plan** plan_out);
 spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream);
 spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
+
+/* ---- tuning ----------------------------------------------------------------------
+ * No counterpart in the reference (its harness sweeps kernels by hand).
+ * The configuration space: a fixed table of spmm_tune_config_count() entries
+ * (37: five mma.sync column tiles and depths; tcgen05 column tiles, depths,
+ * accumulator counts, static or work-queue schedules and split-K). Not every
+ * entry has a kernel for every block height and type. */
+int spmm_tune_config_count(void);
+spmm_status spmm_tune_config(int i, spmm_config* out);
+/* The configuration spmm_bcsr_mm runs when given none (the library's fixed
+ * heuristic), as a table entry. */
+spmm_status spmm_default_config(int bR, spmm_dtype dtype, int N, spmm_config* out);
+/* SPMM_OK if `cfg` has a kernel for (bR, dtype, N), else SPMM_ERR_UNSUPPORTED. */
+spmm_status spmm_config_supported(int bR, spmm_dtype dtype, int N, const spmm_config* cfg);
+/* Exhaustive sweep: times every table entry on this product. Per entry:
+ * `warmup` untimed runs, then `reps` runs each preceded (when flush != NULL)
+ * by a write of flush_bytes to `flush` (evicting L2) and timed alone with CUDA
+ * events; ms_out[i] = the median, +inf where the entry has no kernel.
+ * Overwrites C; synchronises the stream. */
+spmm_status spmm_tune_sweep(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N, float* C, int ldc,
+                            int warmup, int reps, void* flush, size_t flush_bytes, float* ms_out,
+                            void* stream);
+
+/* Structure features (18 floats) of the product A (M x K, bR x 16 blocks,
+ * element type dtype) x B (K x N), the cost model's input. The _host variant
+ * reads host arrays and returns 0 (or -1 on a bad structure); the other copies
+ * row_ptr and col_idx from the device and synchronises the stream. */
+#define SPMM_FEATURES 18
+int spmm_structure_features_host(const int* row_ptr, const int* col_idx, int M, int K, int bR, int N,
+                                 spmm_dtype dtype, float* out);
+spmm_status spmm_structure_features(const spmm_bcsr_desc* A, int N, float* out, void* stream);
+
+/* ---- learned cost model -------------------------------------------------------
+ * No counterpart in the reference. A fp32 MLP: features -> normalisation ->
+ * `layers` hidden layers of `hidden` units with GELU -> `out` outputs,
+ * ln(microseconds) per tuner configuration. Parameters are one flat array
+ * (mu[in], sigma[in], then per layer W[fan_out x fan_in] row-major and
+ * b[fan_out]). Forward, backward (masked mean squared error) and Adam run in
+ * the library's own kernels on device arrays, asynchronously on `stream`. */
+typedef struct spmm_mlp_shape {
+  int in, hidden, layers, out;   /* in, hidden <= 128; out <= 1024; layers <= 16;
+                                    a model for spmm_cost_model_create has in ==
+                                    SPMM_FEATURES and out == spmm_tune_config_count() */
+} spmm_mlp_shape;
+long long spmm_mlp_param_count(const spmm_mlp_shape* shape);
+long long spmm_mlp_workspace_floats(const spmm_mlp_shape* shape, int batch);
+/* Y[batch x out] from X[batch x in]. */
+spmm_status spmm_mlp_forward(const spmm_mlp_shape* shape, const float* params, const float* X, int batch,
+                             float* Y, float* work, void* stream);
+/* loss = sum(mask * (Y - T)^2) / sum(mask) (one float, may be NULL) and
+ * grad = d loss / d params (zero for mu and sigma). */
+spmm_status spmm_mlp_backward(const spmm_mlp_shape* shape, const float* params, const float* X,
+                              const float* T, const float* mask, int batch, float* grad, float* loss,
+                              float* work, void* stream);
+/* One AdamW step (decoupled weight decay) on params[offset, n). step >= 1. */
+spmm_status spmm_mlp_adam(float* params, const float* grad, float* m, float* v, long long n,
+                          long long offset, float lr, float beta1, float beta2, float eps,
+                          float weight_decay, int step, void* stream);
+/* A trained model on the current device (parameters copied from the host;
+ * `out` must equal spmm_tune_config_count()). select computes the features
+ * of A, runs the network and returns the supported configuration with the
+ * smallest predicted time (and, if `predicted_ms` is not NULL, every
+ * entry's prediction in ms, +inf where unsupported). Synchronises the stream. */
+typedef struct spmm_cost_model spmm_cost_model;
+spmm_status spmm_cost_model_create(const spmm_mlp_shape* shape, const float* host_params,
+                                   spmm_cost_model** out);
+spmm_status spmm_cost_model_destroy(spmm_cost_model* model);
+spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr_desc* A, int N,
+                                   spmm_config* out, float* predicted_ms, void* stream);
 
 /* ---- allocation-free variant ---------------------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc (a

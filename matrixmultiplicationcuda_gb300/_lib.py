@@ -31,7 +31,7 @@ class DType(enum.IntEnum):
 
 class Config(ctypes.Structure):
     _fields_ = [("kernel", c_int), ("n_tile", c_int), ("stages", c_int), ("ctas_per_sm", c_int),
-                ("acc_buffers", c_int), ("schedule", c_int)]
+                ("acc_buffers", c_int), ("schedule", c_int), ("split_k", c_int)]
 
 
 class BcsrDesc(ctypes.Structure):
@@ -46,6 +46,10 @@ class DenseDesc(ctypes.Structure):
 
 class Problem(ctypes.Structure):
     _fields_ = [("A", BcsrDesc), ("B", DenseDesc), ("N", c_int), ("C", c_vp), ("ldc", c_int)]
+
+
+class MlpShape(ctypes.Structure):
+    _fields_ = [("in_", c_int), ("hidden", c_int), ("layers", c_int), ("out", c_int)]
 
 
 class SpmmError(RuntimeError):
@@ -79,7 +83,26 @@ _SIGS = {
     "spmm_bcsr_mm_noalloc": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp,
                                      c_int, ctypes.POINTER(Config), c_vp]),
     "spmm_noalloc_error_check": (c_int, [c_vp]),
+    "spmm_tune_config_count": (c_int, []),
+    "spmm_tune_config": (c_int, [c_int, ctypes.POINTER(Config)]),
+    "spmm_default_config": (c_int, [c_int, c_int, c_int, ctypes.POINTER(Config)]),
+    "spmm_config_supported": (c_int, [c_int, c_int, c_int, ctypes.POINTER(Config)]),
+    "spmm_tune_sweep": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp, c_int, c_int,
+                                c_int, c_vp, c_size, c_vp, c_vp]),
+    "spmm_structure_features": (c_int, [ctypes.POINTER(BcsrDesc), c_int, c_vp, c_vp]),
+    "spmm_mlp_param_count": (c_ll, [ctypes.POINTER(MlpShape)]),
+    "spmm_mlp_workspace_floats": (c_ll, [ctypes.POINTER(MlpShape), c_int]),
+    "spmm_mlp_forward": (c_int, [ctypes.POINTER(MlpShape), c_vp, c_vp, c_int, c_vp, c_vp, c_vp]),
+    "spmm_mlp_backward": (c_int, [ctypes.POINTER(MlpShape), c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_vp,
+                                  c_vp]),
+    "spmm_mlp_adam": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_ll, c_float, c_float, c_float, c_float, c_float,
+                              c_int, c_vp]),
+    "spmm_cost_model_create": (c_int, [ctypes.POINTER(MlpShape), c_vp, ctypes.POINTER(c_vp)]),
+    "spmm_cost_model_destroy": (c_int, [c_vp]),
+    "spmm_cost_model_select": (c_int, [c_vp, ctypes.POINTER(BcsrDesc), c_int, ctypes.POINTER(Config), c_vp,
+                                       c_vp]),
     # host side (csrc/host)
+    "spmm_structure_features_host": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp]),
     "spmm_generate_matrix": (c_int, [c_int, c_int, c_double, c_char_p, c_int, c_uint, c_vp]),
     "spmm_gen_structure": (c_ll, [c_int, c_int, c_int, c_int, c_double, c_double, c_ull, c_vp, c_vp]),
     "spmm_gen_values": (None, [c_ll, c_int, c_int, c_int, c_ull, c_vp]),

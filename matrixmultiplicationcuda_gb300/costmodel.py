@@ -1,0 +1,267 @@
+"""The learned cost model: an MLP from structure features to the predicted
+ln(microseconds) of every tuner configuration, trained and run with the
+library's own CUDA kernels (spmm_mlp_forward / _backward / _adam).
+
+Training data are the autotuner's own sweeps on seeded synthetic products
+(collect()); the trained network replaces the sweep at launch
+(CostModel.select), and the sweep stays the fallback and the judge of its
+regret (evaluate()).
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from ._lib import Config, MlpShape, check, lib, stream_handle
+from . import tuner
+from .host import (PATTERN_BAND, PATTERN_BLOCKDIAG, PATTERN_LOGNORMAL, PATTERN_RANDOM, gen_structure)
+
+HIDDEN, LAYERS = 64, 3
+
+
+def shape(n_out=None, n_in=tuner.N_FEATURES, hidden=HIDDEN, layers=LAYERS):
+    s = MlpShape()
+    s.in_, s.hidden, s.layers = n_in, hidden, layers
+    s.out = tuner.n_configs() if n_out is None else n_out
+    return s
+
+
+def param_count(s):
+    return int(lib().spmm_mlp_param_count(ctypes.byref(s)))
+
+
+def init_params(s, mu, sigma, seed=0):
+    """He-style init for the GELU layers, small output layer; mu/sigma from the data."""
+    rng = np.random.default_rng(seed)
+    out = [np.asarray(mu, np.float32), np.asarray(sigma, np.float32)]
+    dims = [s.in_] + [s.hidden] * s.layers + [s.out]
+    for l in range(s.layers + 1):
+        fi, fo = dims[l], dims[l + 1]
+        std = math.sqrt(2.0 / fi) if l < s.layers else math.sqrt(0.5 / fi)
+        out.append((rng.standard_normal((fo, fi)) * std).astype(np.float32).ravel())
+        out.append(np.zeros(fo, np.float32))
+    p = np.concatenate(out)
+    assert p.size == param_count(s)
+    return p
+
+
+def _vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class MLP:
+    """Device-side network (torch float32 buffers, library kernels)."""
+
+    def __init__(self, s, params, device="cuda"):
+        import torch
+        self.s = s
+        self.device = device
+        self.params = torch.as_tensor(np.asarray(params, np.float32)).to(device).contiguous()
+        assert self.params.numel() == param_count(s)
+        self._ws = {}
+
+    def _work(self, batch):
+        import torch
+        if batch not in self._ws:
+            n = int(lib().spmm_mlp_workspace_floats(ctypes.byref(self.s), batch))
+            self._ws[batch] = torch.empty(n, dtype=torch.float32, device=self.device)
+        return self._ws[batch]
+
+    def forward(self, X, stream=None):
+        import torch
+        X = X.contiguous()
+        Y = torch.empty((X.shape[0], self.s.out), dtype=torch.float32, device=self.device)
+        check(lib().spmm_mlp_forward(ctypes.byref(self.s), _vp(self.params), _vp(X), X.shape[0], _vp(Y),
+                                     _vp(self._work(X.shape[0])), stream_handle(stream)))
+        return Y
+
+    def loss_grad(self, X, T, mask, stream=None):
+        import torch
+        X, T, mask = X.contiguous(), T.contiguous(), mask.contiguous()
+        g = torch.empty_like(self.params)
+        loss = torch.zeros(1, dtype=torch.float32, device=self.device)
+        check(lib().spmm_mlp_backward(ctypes.byref(self.s), _vp(self.params), _vp(X), _vp(T), _vp(mask),
+                                      X.shape[0], _vp(g), _vp(loss), _vp(self._work(X.shape[0])),
+                                      stream_handle(stream)))
+        return loss, g
+
+    def train(self, X, T, mask, steps=3000, batch=256, lr=2e-3, wd=1e-4, seed=0, log_every=0):
+        """AdamW on mini-batches drawn with a seeded permutation; cosine decay."""
+        import torch
+        n = X.shape[0]
+        m = torch.zeros_like(self.params)
+        v = torch.zeros_like(self.params)
+        off = 2 * self.s.in_
+        rng = np.random.default_rng(seed)
+        order = rng.permutation(n)
+        pos = 0
+        losses = []
+        for step in range(1, steps + 1):
+            if pos + batch > n:
+                order = rng.permutation(n)
+                pos = 0
+            idx = torch.as_tensor(order[pos:pos + batch], device=self.device)
+            pos += batch
+            loss, g = self.loss_grad(X[idx], T[idx], mask[idx])
+            lr_t = lr * 0.5 * (1 + math.cos(math.pi * step / steps))
+            check(lib().spmm_mlp_adam(_vp(self.params), _vp(g), _vp(m), _vp(v), self.params.numel(), off,
+                                      lr_t, 0.9, 0.999, 1e-8, wd, step, stream_handle(None)))
+            if log_every and step % log_every == 0:
+                losses.append(float(loss))
+        return losses
+
+    def host_params(self):
+        return self.params.cpu().numpy()
+
+
+class CostModel:
+    """A trained network loaded into the library (spmm_cost_model_select)."""
+
+    def __init__(self, s, params):
+        self.s = s
+        p = np.ascontiguousarray(params, np.float32)
+        h = ctypes.c_void_p()
+        check(lib().spmm_cost_model_create(ctypes.byref(s), ctypes.c_void_p(p.ctypes.data), ctypes.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def load(path):
+        z = np.load(path)
+        dims = z["shape"]
+        s = shape(n_out=int(dims[3]), n_in=int(dims[0]), hidden=int(dims[1]), layers=int(dims[2]))
+        return CostModel(s, z["params"])
+
+    def select(self, A, N, stream=None, return_predictions=False):
+        c = Config()
+        pred = np.zeros(self.s.out, np.float32)
+        d = A.desc()
+        check(lib().spmm_cost_model_select(self._h, ctypes.byref(d), int(N), ctypes.byref(c),
+                                           ctypes.c_void_p(pred.ctypes.data), stream_handle(stream)))
+        return (c, pred) if return_predictions else c
+
+    def close(self):
+        if self._h:
+            lib().spmm_cost_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def save(path, s, params, **extra):
+    np.savez(path, shape=np.array([s.in_, s.hidden, s.layers, s.out], np.int32),
+             params=np.asarray(params, np.float32), **extra)
+
+
+# ---- training data: sweeps on seeded synthetic products --------------------------
+
+def sample_specs(n, seed):
+    """Products drawn like the three single-product workloads: the 1024^2
+    16x16 random case (sizes 512..2048), the 8192^2 sweep (block heights 16,
+    32, 64; random, band, block-diagonal and log-normal clustered patterns;
+    N 256..4096) and the 16384^2 64x16 case (N 512), with densities
+    log-uniform in [0.5 %, 25 %]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n):
+        u = rng.uniform()
+        if u < 0.2:
+            M = int(rng.choice([512, 1024, 1536, 2048]))
+            N = int(rng.choice([128, 256, 512, 1024]))
+            bR = int(rng.choice([16, 32, 64]))
+        elif u < 0.8:
+            M = int(rng.choice([2048, 4096, 6144, 8192]))
+            N = int(rng.choice([256, 512, 1024, 2048, 4096]))
+            bR = int(rng.choice([16, 32, 64]))
+        else:
+            M = int(rng.choice([12288, 16384]))
+            N = int(rng.choice([256, 512, 1024]))
+            bR = int(rng.choice([32, 64, 64]))
+        pattern = int(rng.choice([PATTERN_RANDOM, PATTERN_BAND, PATTERN_BLOCKDIAG, PATTERN_LOGNORMAL]))
+        density = float(math.exp(rng.uniform(math.log(0.005), math.log(0.25))))
+        KB = M // 16
+        if pattern == PATTERN_BAND:
+            param = float(rng.choice([8, max(1, int(density * KB / 2))]))
+        elif pattern == PATTERN_BLOCKDIAG:
+            param = float(max(64, int(round(density * M / 64)) * 64))
+        elif pattern == PATTERN_LOGNORMAL:
+            param = float(rng.uniform(0.5, 2.0))
+        else:
+            param = 0.0
+        dtype = int(rng.choice([0, 1, 2, 3], p=[0.55, 0.15, 0.15, 0.15]))
+        specs.append(dict(M=M, K=M, N=N, bR=bR, pattern=pattern, density=density, param=param,
+                          seed=seed * 100003 + i, dtype=dtype))
+    return specs
+
+
+def collect(specs, warmup=2, reps=5, device="cuda", progress=None):
+    """Features [n x 18], sweep times [n x configs] (ms, +inf unsupported) and
+    stored-block counts of the products in `specs`. Values come from fixed
+    random pools (timing does not depend on them; e4m3 operands are the same
+    bytes reinterpreted, split products reuse them as the low halves); the
+    structure is generated per product."""
+    import torch
+    from .bcsr import BCSR
+    from ._lib import DType
+    maxM = max(s["M"] for s in specs)
+    maxN = max(s["N"] for s in specs)
+    max_vals = max((s["M"] // s["bR"]) * (s["K"] // 16) * s["bR"] * 16 for s in specs)
+    g = torch.Generator(device=device).manual_seed(1)
+    pool = (torch.rand(min(max_vals, 96 << 20), generator=g, device=device) * 2 - 1).half()
+    Bpool = (torch.rand(maxM * maxN, generator=g, device=device) * 2 - 1).half()
+    scales = torch.ones(max(max_vals // 256, 1), dtype=torch.float32, device=device)
+    Cbuf = torch.empty(maxM * maxN, dtype=torch.float32, device=device)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    F = np.zeros((len(specs), tuner.N_FEATURES), np.float32)
+    T = np.zeros((len(specs), tuner.n_configs()), np.float32)
+    nnzb = np.zeros(len(specs), np.int64)
+    for k, s in enumerate(specs):
+        dt = DType(s.get("dtype", 0))
+        rp, ci = gen_structure(s["M"], s["K"], s["bR"], s["pattern"], s["density"], s["param"], seed=s["seed"])
+        nvals = len(ci) * s["bR"] * 16
+        if nvals > pool.numel():
+            raise ValueError("value pool too small")
+        rpd, cid = torch.as_tensor(rp).to(device), torch.as_tensor(ci).to(device)
+        KN = s["K"] * s["N"]
+        B_lo = None
+        if dt == DType.E4M3:
+            A = BCSR(s["M"], s["K"], s["bR"], 16, rpd, cid, pool.view(torch.uint8)[:nvals], dt,
+                     scales=scales[:max(len(ci), 1)])
+            B = Bpool.view(torch.uint8)[:KN].view(s["K"], s["N"])
+        else:
+            v = pool[:nvals] if dt != DType.BF16 else pool[:nvals].view(torch.bfloat16)
+            A = BCSR(s["M"], s["K"], s["bR"], 16, rpd, cid, v, dt,
+                     vals_lo=pool[:nvals] if dt == DType.F16_SPLIT else None)
+            B = Bpool[:KN].view(s["K"], s["N"])
+            if dt == DType.BF16:
+                B = B.view(torch.bfloat16)
+            if dt == DType.F16_SPLIT:
+                B_lo = B
+        C = Cbuf[:s["M"] * s["N"]].view(s["M"], s["N"])
+        F[k] = tuner.features_host(rp, ci, s["M"], s["K"], s["bR"], s["N"], dt)
+        T[k] = tuner.sweep(A, B, s["N"], C, warmup, reps, flush, B_lo=B_lo)
+        nnzb[k] = len(ci)
+        if progress and (k + 1) % progress == 0:
+            print("collected %d / %d" % (k + 1, len(specs)), flush=True)
+    return F, T, nnzb
+
+
+def targets(T_ms):
+    """ln(microseconds) targets and the mask of measured entries."""
+    mask = np.isfinite(T_ms)
+    Tl = np.where(mask, np.log(np.where(mask, T_ms, 1.0) * 1e3), 0.0).astype(np.float32)
+    return Tl, mask.astype(np.float32)
+
+
+def regret(T_ms, pick):
+    """t(pick) / t(best) - 1 per product."""
+    best = np.min(T_ms, axis=1)
+    chosen = T_ms[np.arange(len(pick)), pick]
+    return chosen / best - 1.0
+
+
+def picks_from_predictions(pred, mask):
+    return np.argmin(np.where(mask > 0, pred, np.inf), axis=1)

@@ -84,6 +84,18 @@ const Entry* find_entry(int br, int mode, int nt, int stages) {
 
 }  // namespace
 
+int mma_default_nt(int bR, spmm_dtype dtype, int N) {
+  const int mode = mode_of(dtype);
+  return mode < 0 ? 0 : default_nt(bR, mode, N);
+}
+
+bool mma_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg) {
+  const int mode = mode_of(dtype);
+  if (mode < 0) return false;
+  const int nt = cfg.n_tile > 0 ? cfg.n_tile : default_nt(bR, mode, N);
+  return find_entry(bR, mode, nt, cfg.stages) != nullptr;
+}
+
 spmm_status launch_mma(const LaunchRequest& r) {
   const spmm_bcsr_desc& A = *r.A;
   const spmm_dense_desc& B = *r.B;

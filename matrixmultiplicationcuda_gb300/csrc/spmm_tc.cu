@@ -53,6 +53,7 @@ struct TcParams {
   unsigned* err;
   int panel3d;      // B panel loaded by one 3-D copy (N % 64 == 0)
   unsigned* queue;  // [0] next item, [1] CTAs done; NULL = static item striding
+  int split;        // items per (block row, column tile); > 1: partial sums added into C
 };
 
 // BR: block height (the UMMA N); NT: output columns per item; STAGES: ring
@@ -171,12 +172,29 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       };
       uint32_t gs = 0, it = 0;
       bool failed = false;
+      // block range of an item: its block row's range, or one of p.split
+      // slices of it (slice lengths a multiple of 4 blocks, so that only a
+      // row's last slice can end in a partial group)
+      auto range = [&](int v, int* s0, int* s1) {
+        if (v < 0) {
+          *s0 = *s1 = 0;
+          return;
+        }
+        const int row = v / (p.ntiles * p.split);
+        int a = __ldg(p.row_ptr + row), b = __ldg(p.row_ptr + row + 1);
+        if (p.split > 1) {
+          const int k = v % p.split;
+          const int chunk = (((b - a) + p.split - 1) / p.split + 3) & ~3;
+          const int a2 = min(b, a + k * chunk);
+          b = min(b, a2 + chunk);
+          a = a2;
+        }
+        *s0 = a;
+        *s1 = b;
+      };
       int item = next_item(-1);
       int start = 0, end = 0;
-      if (item >= 0) {
-        start = __ldg(p.row_ptr + item / p.ntiles);
-        end = __ldg(p.row_ptr + item / p.ntiles + 1);
-      }
+      range(item, &start, &end);
       for (;; ++it) {
         const uint32_t q = it % kQ;
         if (it >= (uint32_t)kQ && !mbar_wait(qempty0 + 8 * q, ((it / kQ) + 1) & 1, p.timeout_ns)) {
@@ -190,10 +208,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         if (item < 0 || failed) break;
         const int nitem = next_item(item);
         int nstart = 0, nend = 0;
-        if (nitem >= 0) {
-          nstart = __ldg(p.row_ptr + nitem / p.ntiles);
-          nend = __ldg(p.row_ptr + nitem / p.ntiles + 1);
-        }
+        range(nitem, &nstart, &nend);
         for (int j0 = start; j0 < end; j0 += G, ++gs) {
           const int n = min(G, end - j0);
           const int s = (int)(gs % STAGES);
@@ -252,7 +267,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       start = __shfl_sync(0xffffffffu, start, 0);
       end = __shfl_sync(0xffffffffu, end, 0);
       if (!ok || item < 0) break;
-      const int nt = item - (item / p.ntiles) * p.ntiles;
+      const int nt = (item / p.split) % p.ntiles;
       int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
@@ -362,7 +377,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       item = __shfl_sync(0xffffffffu, item, 0);
       const bool empty = __shfl_sync(0xffffffffu, start == end ? 1 : 0, 0) != 0;
       if (!ok || item < 0) break;
-      const int br = item / p.ntiles, nt = item - br * p.ntiles;
+      const int br = item / (p.ntiles * p.split), nt = (item / p.split) % p.ntiles;
       const uint32_t acc = it % ACC;
       if (!mbar_wait(tfull0 + 8 * acc, (it / ACC) & 1, p.timeout_ns)) {
         if (lane == 0) atomicOr(p.err, 16u);
@@ -385,8 +400,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             for (int i = 0; i < 16; ++i) v[i] = 0.f;
           }
           if (n < p.N) {
+            if (p.split == 1) {
 #pragma unroll
-            for (int i = 0; i < 16; ++i) __stcs(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+              for (int i = 0; i < 16; ++i) __stcs(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+            } else if (!empty) {
+#pragma unroll
+              for (int i = 0; i < 16; ++i) atomicAdd(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+            }
           }
         }
       }
@@ -435,26 +455,44 @@ const TcEntry kTcEntries[] = {
     SPMM_TC_ENTRY(64, 512, 2, MODE_SPLIT, 1, 1),
 };
 
+int tc_mode(spmm_dtype d) {
+  return d == SPMM_F16 ? MODE_F16 : d == SPMM_BF16 ? MODE_BF16 : d == SPMM_F16_SPLIT ? MODE_SPLIT : -1;
+}
+
+// The instantiation a request runs on (NULL if none): column tile (default 128
+// for 64-row blocks and N <= 128, else 256), then the first entry matching the
+// requested depth and accumulator count.
+const TcEntry* find_tc(int bR, int mode, int N, const spmm_config& cfg, int* nt_out) {
+  int nt = cfg.n_tile;
+  if (nt <= 0) nt = (N <= 128 && bR == 64) ? 128 : 256;
+  if (nt < 256 && bR != 64) nt = 256;
+  *nt_out = nt;
+  for (const TcEntry& c : kTcEntries) {
+    if (c.br != bR || c.mode != mode || c.nt != nt) continue;
+    if (cfg.stages > 0 && c.stages != cfg.stages) continue;
+    if (cfg.acc_buffers > 0 && c.acc != cfg.acc_buffers) continue;
+    return &c;
+  }
+  return nullptr;
+}
+
 }  // namespace
+
+bool tc_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg) {
+  const int mode = tc_mode(dtype);
+  int nt = 0;
+  // a requested column tile must be the one that runs (find_tc widens 128 to 256 for 16- and 32-row blocks)
+  return mode >= 0 && cfg.split_k <= 16 && find_tc(bR, mode, N, cfg, &nt) != nullptr &&
+         (cfg.n_tile <= 0 || nt == cfg.n_tile);
+}
 
 spmm_status launch_tc(const LaunchRequest& r) {
   const spmm_bcsr_desc& A = *r.A;
   const spmm_dense_desc& B = *r.B;
-  int mode = A.dtype == SPMM_F16 ? MODE_F16 : A.dtype == SPMM_BF16 ? MODE_BF16
-                                               : A.dtype == SPMM_F16_SPLIT ? MODE_SPLIT : -1;
+  const int mode = tc_mode(A.dtype);
   if (mode < 0) return fail(SPMM_ERR_UNSUPPORTED, "tcgen05 pipeline: fp16, bf16 and split fp16 only");
-  int nt = r.cfg.n_tile;
-  if (nt <= 0) nt = (r.N <= 128 && A.bR == 64) ? 128 : 256;
-  if (nt < 256 && A.bR != 64) nt = 256;
-  const int acc = r.cfg.acc_buffers;
-  const TcEntry* e = nullptr;
-  for (const TcEntry& c : kTcEntries) {
-    if (c.br != A.bR || c.mode != mode || c.nt != nt) continue;
-    if (r.cfg.stages > 0 && c.stages != r.cfg.stages) continue;
-    if (acc > 0 && c.acc != acc) continue;
-    e = &c;
-    break;
-  }
+  int nt = 0;
+  const TcEntry* e = find_tc(A.bR, mode, r.N, r.cfg, &nt);
   if (!e)
     return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for bR=" + std::to_string(A.bR) +
                                           " n_tile=" + std::to_string(nt));
@@ -507,7 +545,11 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.ldc = r.ldc;
   p.N = r.N;
   p.ntiles = (r.N + nt - 1) / nt;
-  p.n_items = (A.M / A.bR) * p.ntiles;
+  p.split = r.cfg.split_k > 1 ? r.cfg.split_k : 1;
+  if (p.split > 16) return fail(SPMM_ERR_INVALID_ARG, "split_k must be at most 16");
+  const long long n_items = (long long)(A.M / A.bR) * p.ntiles * p.split;
+  if (n_items >= (1ll << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
+  p.n_items = (int)n_items;
   p.timeout_ns = wait_limit_ns();
   p.err = r.err_word ? r.err_word : device_error_word();
   p.panel3d = panel3d;
@@ -515,6 +557,8 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
+  if (p.split > 1)
+    SPMM_CUDA_TRY(cudaMemset2DAsync(r.C, (size_t)r.ldc * 4, 0, (size_t)r.N * 4, A.M, r.stream));
   SPMM_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(e->fn),
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
   // CTAs per SM from the real limits: TMEM columns (512 per SM), shared memory
@@ -534,9 +578,9 @@ spmm_status launch_tc(const LaunchRequest& r) {
   if (std::getenv("SPMM_DEBUG"))
     std::fprintf(stderr,
                  "[spmm] tcgen05 bR=%d nt=%d stages=%d acc=%d group=%d smem=%zu tmem=%d per_sm=%d grid=%lld "
-                 "items=%d panel3d=%d queue=%d\n",
+                 "items=%d panel3d=%d queue=%d split=%d\n",
                  A.bR, nt, e->stages, e->acc, e->group, e->smem, e->tmem_cols, per_sm, grid, p.n_items, panel3d,
-                 p.queue != nullptr);
+                 p.queue != nullptr, p.split);
   e->fn<<<(unsigned)grid, kTcThreads, e->smem, r.stream>>>(tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo, p);
   SPMM_CUDA_TRY(cudaGetLastError());
   return SPMM_OK;

@@ -1,0 +1,156 @@
+// The tuner's configuration space, the exhaustive sweep over it, and the
+// device-array wrapper of the structure features.
+//
+// The table has 37 entries: five mma.sync tiles (column tile x ring depth)
+// and 32 tcgen05 variants (column tile, ring depth, TMEM accumulators, static
+// or work-queue schedule, split-K of 1, 2, 4 and, for the default 256-column
+// tile, 8). Which entries have a kernel depends on the block height and the
+// type; spmm_config_supported answers that without launching.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "internal.h"
+
+namespace spmm {
+namespace {
+
+std::vector<spmm_config> make_table() {
+  std::vector<spmm_config> t;
+  auto add = [&](int kernel, int nt, int stages, int acc, int sched, int split) {
+    spmm_config c;
+    std::memset(&c, 0, sizeof(c));
+    c.kernel = kernel;
+    c.n_tile = nt;
+    c.stages = stages;
+    c.acc_buffers = acc;
+    c.schedule = sched;
+    c.split_k = split;
+    t.push_back(c);
+  };
+  add(1, 64, 4, 0, 0, 0);
+  add(1, 128, 4, 0, 0, 0);
+  add(1, 128, 8, 0, 0, 0);
+  add(1, 256, 4, 0, 0, 0);
+  add(1, 256, 8, 0, 0, 0);
+  struct Tc {
+    int nt, stages, acc, max_split;
+  };
+  const Tc tcs[] = {{128, 0, 2, 4}, {256, 0, 2, 8}, {256, 2, 2, 4}, {512, 0, 1, 4}, {512, 0, 2, 4}};
+  for (const Tc& x : tcs)
+    for (int sched = 0; sched < 2; ++sched)
+      for (int split = 1; split <= x.max_split; split *= 2) add(2, x.nt, x.stages, x.acc, sched, split);
+  return t;
+}
+
+const std::vector<spmm_config>& table() {
+  static const std::vector<spmm_config> t = make_table();
+  return t;
+}
+
+}  // namespace
+}  // namespace spmm
+
+using namespace spmm;
+
+extern "C" {
+
+int spmm_tune_config_count(void) { return (int)table().size(); }
+
+spmm_status spmm_tune_config(int i, spmm_config* out) {
+  if (!out || i < 0 || i >= (int)table().size()) return fail(SPMM_ERR_INVALID_ARG, "config index out of range");
+  *out = table()[i];
+  return SPMM_OK;
+}
+
+spmm_status spmm_config_supported(int bR, spmm_dtype dtype, int N, const spmm_config* cfg) {
+  if (!cfg) return fail(SPMM_ERR_INVALID_ARG, "null config");
+  bool ok = false;
+  if (cfg->kernel == 1) ok = cfg->split_k <= 1 && mma_supported(bR, dtype, N, *cfg);
+  else if (cfg->kernel == 2) ok = tc_supported(bR, dtype, N, *cfg);
+  return ok ? SPMM_OK : SPMM_ERR_UNSUPPORTED;
+}
+
+spmm_status spmm_default_config(int bR, spmm_dtype dtype, int N, spmm_config* out) {
+  if (!out) return fail(SPMM_ERR_INVALID_ARG, "null config");
+  spmm_config c;
+  std::memset(&c, 0, sizeof(c));
+  // spmm_bcsr_mm with no configuration: the tcgen05 pipeline for 64-row
+  // blocks where it has a kernel (its first instantiation for the column tile:
+  // two accumulators, static schedule), else the mma.sync pipeline (depth 4).
+  if (bR == 64 && tc_supported(bR, dtype, N, c)) {
+    c.kernel = 2;
+    c.n_tile = N <= 128 ? 128 : 256;
+    c.acc_buffers = 2;
+    c.split_k = 1;
+  } else {
+    c.kernel = 1;
+    c.n_tile = mma_default_nt(bR, dtype, N);
+    c.stages = 4;
+  }
+  *out = c;
+  return spmm_config_supported(bR, dtype, N, &c) == SPMM_OK ? SPMM_OK
+                                                            : fail(SPMM_ERR_UNSUPPORTED, "no default kernel");
+}
+
+spmm_status spmm_tune_sweep(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N, float* C, int ldc,
+                            int warmup, int reps, void* flush, size_t flush_bytes, float* ms_out,
+                            void* stream) {
+  if (!A || !B || !ms_out || reps < 1 || warmup < 0) return fail(SPMM_ERR_INVALID_ARG, "bad sweep arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0, e1;
+  SPMM_CUDA_TRY(cudaEventCreate(&e0));
+  SPMM_CUDA_TRY(cudaEventCreate(&e1));
+  std::vector<float> ts(reps);
+  spmm_status result = SPMM_OK;
+  for (size_t i = 0; i < table().size() && result == SPMM_OK; ++i) {
+    const spmm_config& c = table()[i];
+    if (spmm_config_supported(A->bR, A->dtype, N, &c) != SPMM_OK) {
+      ms_out[i] = INFINITY;
+      continue;
+    }
+    for (int w = 0; w < warmup && result == SPMM_OK; ++w) result = spmm_bcsr_mm(A, B, N, C, ldc, &c, stream);
+    for (int k = 0; k < reps && result == SPMM_OK; ++k) {
+      if (flush && flush_bytes) {
+        cudaError_t ce = cudaMemsetAsync(flush, k & 0xff, flush_bytes, s);
+        if (ce != cudaSuccess) result = cuda_fail(ce, "flushing L2");
+      }
+      cudaEventRecord(e0, s);
+      if (result == SPMM_OK) result = spmm_bcsr_mm(A, B, N, C, ldc, &c, stream);
+      cudaEventRecord(e1, s);
+      cudaError_t ce = cudaEventSynchronize(e1);
+      if (ce != cudaSuccess && result == SPMM_OK) result = cuda_fail(ce, "timing a configuration");
+      if (result == SPMM_OK) cudaEventElapsedTime(&ts[k], e0, e1);
+    }
+    if (result == SPMM_OK) {
+      std::sort(ts.begin(), ts.end());
+      ms_out[i] = ts[reps / 2];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return result;
+}
+
+spmm_status spmm_structure_features(const spmm_bcsr_desc* A, int N, float* out, void* stream) {
+  if (!A || !out || !A->row_ptr || A->bR <= 0 || A->M <= 0 || A->M % A->bR)
+    return fail(SPMM_ERR_INVALID_ARG, "bad features arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int MB = A->M / A->bR;
+  std::vector<int> rp(MB + 1);
+  SPMM_CUDA_TRY(cudaMemcpyAsync(rp.data(), A->row_ptr, sizeof(int) * (MB + 1), cudaMemcpyDeviceToHost, s));
+  SPMM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (rp[0] != 0 || rp[MB] < 0) return fail(SPMM_ERR_BAD_STRUCTURE, "row_ptr[0] != 0");
+  const long long nnzb = rp[MB];
+  std::vector<int> ci((size_t)std::max<long long>(nnzb, 1));
+  if (nnzb > 0) {
+    if (!A->col_idx) return fail(SPMM_ERR_INVALID_ARG, "null col_idx");
+    SPMM_CUDA_TRY(cudaMemcpyAsync(ci.data(), A->col_idx, sizeof(int) * nnzb, cudaMemcpyDeviceToHost, s));
+    SPMM_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  if (spmm_structure_features_host(rp.data(), ci.data(), A->M, A->K, A->bR, N, A->dtype, out) != 0)
+    return fail(SPMM_ERR_BAD_STRUCTURE, "row_ptr / col_idx out of range");
+  return SPMM_OK;
+}
+
+}  // extern "C"

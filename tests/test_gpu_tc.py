@@ -81,3 +81,29 @@ def test_tc_short_rows_repeated(dev, queue):
     ref = oracle.bcsr_matmul_f64(rp, ci, rounded(vals, "f16"), bR, 16, rounded(Bf, "f16"))
     mx, fr = oracle.rel_errors(C.cpu().numpy(), ref)
     assert mx <= 1e-5 and fr <= 1e-5, (mx, fr)
+
+
+@pytest.mark.parametrize("bR,nt,name,acc", [(64, 256, "f16", 2), (64, 512, "f16", 1), (32, 256, "bf16", 2),
+                                            (16, 512, "f16", 1), (64, 256, "split", 2)])
+@pytest.mark.parametrize("split,queue", [(2, 0), (3, 1), (8, 1), (16, 0)])
+def test_tc_split_k(dev, bR, nt, name, acc, split, queue):
+    """Split-K: each block row's blocks spread over `split` items whose partial
+    products are added into a zeroed C. Rows of 0 to ~200 blocks, so some
+    slices are empty and some end in a partial group."""
+    M, K, N = 512, 8192, 256
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, 0.2, 1.5, seed=bR + split)
+    vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=5)
+    Bf = m.gen_dense(K, N, m.DIST_UNIFORM, seed=6)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, DT[name], device=dev)
+    Bq, Blo, _ = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), DT[name])
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    m.spmm(A, Bq.view(K, N), N=N, C=C, B_lo=Blo.view(K, N) if Blo is not None else None,
+           cfg=m.Config(kernel=2, n_tile=nt, acc_buffers=acc, schedule=queue, split_k=split))
+    m.device_error_check()
+    got = C.cpu().numpy()
+    ref = oracle.bcsr_matmul_f64(rp, ci, rounded(vals, name), bR, 16, rounded(Bf, name))
+    mx, fr = oracle.rel_errors(got, ref)
+    assert np.isfinite(got).all()
+    assert mx <= 3e-5 and fr <= 3e-5, (mx, fr)
+    for br in np.nonzero(np.diff(rp) == 0)[0][:4]:
+        assert np.all(got[br * bR:(br + 1) * bR] == 0)
