@@ -9,11 +9,16 @@ Workload (the mixed-precision configuration the headline metric is quoted on):
   step's data from L2.
 
 Arms:
-  (default) this library: every precision (fp16, bf16, e4m3 + per-block scales,
-            split fp16 hi+lo) is autotuned over the kernel configurations; the
-            headline `value` is the fastest precision whose documented error bar
-            (tests/test_gpu_precision.py) is <= 1e-2 relative to FP64; plain fp16
-            is reported beside it.
+  (default) this library: for every precision (fp16, bf16, e4m3 + per-block
+            scales, split fp16 hi+lo) the learned cost model picks the kernel
+            configuration (the exhaustive sweep over the 37 configurations runs
+            beside it and is reported as the model's regret); the headline `value`
+            is the fastest precision whose documented error bar
+            (tests/test_gpu_precision.py) is <= 1e-2 relative to FP64. Plain fp16
+            (the library's default configuration, no tuning) is reported beside it.
+            The line also carries the batched workload: 64 uneven products in one
+            persistent launch replayed from a CUDA graph, against 64 sequential
+            launches.
   --impl reference: the reference's host multiply (cpu_matmul_ref,
             nvbench_main.cu:78-91, restated in oracle/) on all host cores, over a
             bounded row sample per step, in the same unit.
@@ -228,6 +233,7 @@ def run_reference(args, world, rank):
         t_total += time.perf_counter() - t0
         f_total += useful_flops_rows(rp, r0, rows)
     value = f_total / t_total / 1e12
+    wmma = reference_wmma_gpu(rp, ci, vals, B)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -236,8 +242,46 @@ def run_reference(args, world, rank):
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                              "sample": "%d of %d output rows per step, reference host multiply "
                                        "(dense i-k-j, fp32) split by rows over %d threads" % (rows, M, threads)},
-            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_wmma_gpu": wmma}
     print(json.dumps(line))
+
+
+def reference_wmma_gpu(rp, ci, vals, B, reps=20):
+    """The reference's own WMMA kernel for 64x16 blocks (sparseMatrixMulTensor64x16,
+    src/cuda_kernels.cu:618-695, built unmodified for sm_103a), launched with the
+    reference harness's grid on the same workload, timed with CUDA events on a
+    cold L2. None when no GPU or no reference build is present."""
+    try:
+        import torch
+        from oracle import oracle
+        if not torch.cuda.is_available() or not oracle.ref_wmma_available():
+            return None
+    except ImportError:
+        return None
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d = [t(rp), t(ci), t(vals.astype(np.float16)), t(B)]
+    C = torch.empty((M, N), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    launch = lambda: oracle.ref_wmma_launch("sparseMatrixMulTensor64x16", d[0].data_ptr(), d[1].data_ptr(),
+                                            d[2].data_ptr(), d[3].data_ptr(), C.data_ptr(), M, N, st)
+    for _ in range(3):
+        launch()
+    ts = []
+    for k in range(reps):
+        flush.fill_(k & 0xff)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e3)
+    us = float(np.median(ts))
+    flops = 2.0 * len(ci) * BR * 16 * N
+    return {"kernel": "sparseMatrixMulTensor64x16", "us": us, "tflops": flops / (us * 1e-6) / 1e12,
+            "grid": "(N/32, M/64) warps of 32 threads, as the reference harness launches it"}
 
 
 def run_ours(args, world, rank, local):
@@ -295,10 +339,12 @@ def run_ours(args, world, rank, local):
         e1.synchronize()
         return e0.elapsed_time(e1) / steps
 
-    # autotune every precision over the instantiated kernel configurations
-    cands = [m.Config(kernel=k, n_tile=nt, stages=st, acc_buffers=acc, schedule=sch) for k, nt, st, acc, sch in
-             [(2, 256, 4, 2, 0), (2, 256, 4, 2, 1), (2, 256, 2, 2, 0), (2, 512, 3, 1, 0), (2, 512, 3, 2, 0),
-              (2, 128, 4, 2, 0), (1, 128, 8, 0, 0), (1, 128, 4, 0, 0), (1, 64, 4, 0, 0)]]
+    # Per precision: the learned cost model's pick, timed; the exhaustive sweep
+    # beside it (its best, and the model's regret against it).
+    from matrixmultiplicationcuda_gb300 import costmodel, tuner
+    model = costmodel.CostModel.load(os.path.join(ROOT, "matrixmultiplicationcuda_gb300", "data", "costmodel.npz"))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    table = tuner.configs()
     results = {}
     prepared = {}
     sampler = ClockSampler(local)
@@ -307,19 +353,24 @@ def run_ours(args, world, rank, local):
     for name, dt in precs.items():
         probs = prepare(dt)
         prepared[name] = probs
-        best = None
-        for cfg in cands:
-            try:
-                time_loop(probs, cfg, 3)
-                m.device_error_check()
-            except m.SpmmError:
-                continue
-            t = time_loop(probs, cfg, 30)
-            sys.stderr.write("tune %s kernel=%d n_tile=%d stages=%d acc=%d schedule=%d: %.2f us\n" % (name, cfg.kernel, cfg.n_tile, cfg.stages, cfg.acc_buffers, cfg.schedule, t * 1e3))
-            if best is None or t < best[0]:
-                best = (t, cfg)
-        results[name] = {"ms": best[0], "cfg": best[1], "tflops": flops / best[0] / 1e9,
+        A0, Bq0, Blo0, _, C0 = probs[0]
+        ms_sweep = tuner.sweep(A0, Bq0, N, C0, warmup=2, reps=5, flush=flush, B_lo=Blo0)
+        cfg_model = model.select(A0, N)
+        cfg_sweep = table[int(np.argmin(ms_sweep))]
+        time_loop(probs, cfg_model, 3)
+        time_loop(probs, cfg_sweep, 3)
+        t_model = time_loop(probs, cfg_model, 30)
+        t_sweep = time_loop(probs, cfg_sweep, 30)
+        m.device_error_check()
+        sys.stderr.write("%s: model pick %s %.2f us, sweep best %s %.2f us\n" % (
+            name, tuner.config_name(cfg_model), t_model * 1e3, tuner.config_name(cfg_sweep), t_sweep * 1e3))
+        results[name] = {"ms": t_model, "cfg": cfg_model, "tflops": flops / t_model / 1e9,
+                         "sweep_ms": t_sweep, "sweep_cfg": cfg_sweep,
                          "err_bar": ERROR_BAR[name], "bytes": algorithmic_bytes(nnzb, cols_touched, name)}
+    model.close()
+    # plain fp16: the library's default configuration, no tuning
+    time_loop(prepared["f16"], None, 3)
+    plain_ms = time_loop(prepared["f16"], None, 30)
     ok = {k: v for k, v in results.items() if v["err_bar"] <= TARGET_ERR}
     tuned = min(ok, key=lambda k: results[k]["ms"])
     probs, cfg = prepared[tuned], results[tuned]["cfg"]
@@ -402,6 +453,8 @@ def run_ours(args, world, rank, local):
     sampler.stop()
     clocks = sampler.summary()
 
+    batched = None if args.no_batch else bench_batched(m, torch, dev, flush, hbm_peak)
+
     # CPU baseline (reference host multiply, restated), rank 0 only, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -425,16 +478,19 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": tuned, "data": "synthetic (seeded generators)",
             "config": {"workload": WORKLOAD, "precision": tuned,
-                       "kernel_config": {"kernel": cfg.kernel, "n_tile": cfg.n_tile, "stages": cfg.stages,
-                                         "acc_buffers": cfg.acc_buffers, "schedule": cfg.schedule},
+                       "kernel_config": tuner.config_name(cfg), "picked_by": "learned cost model",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
                        "nnzb": nnzb},
-            "plain_fp16": {"tflops": results["f16"]["tflops"], "ms": results["f16"]["ms"]},
-            "tuned_vs_plain_fp16": results["f16"]["ms"] / tr["ms"],
+            "plain_fp16": {"tflops": flops / plain_ms / 1e9, "ms": plain_ms,
+                           "kernel_config": "library default (no tuning)"},
+            "tuned_vs_plain_fp16": plain_ms / tr["ms"],
             "precisions": {k: {"tflops": v["tflops"], "ms": v["ms"], "err_bar": v["err_bar"],
-                               "kernel": v["cfg"].kernel, "n_tile": v["cfg"].n_tile, "stages": v["cfg"].stages}
+                               "model_pick": tuner.config_name(v["cfg"]),
+                               "sweep_best": tuner.config_name(v["sweep_cfg"]), "sweep_best_ms": v["sweep_ms"],
+                               "model_regret": v["ms"] / v["sweep_ms"] - 1.0}
                            for k, v in results.items()},
+            "batched": batched,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
                          "algorithmic_bytes": bytes_launch, "peak_source": peak_kind,
@@ -446,6 +502,67 @@ def run_ours(args, world, rank, local):
             "clocks": clocks,
         }
         print(json.dumps(line))
+
+
+def bench_batched(m, torch, dev, flush, hbm_peak, reps=20):
+    """64 uneven fp16 products (workloads.uneven_batch_specs): one persistent
+    launch replayed from a CUDA graph against 64 sequential single-product
+    launches (eager and graph-captured), L2 flushed before every timed run."""
+    specs = m.uneven_batch_specs(64, seed=2024)
+    probs, flops, nbytes = [], 0.0, 0.0
+    for sp in specs:
+        rp, ci, vals, Bf = m.make_problem(sp)
+        A = m.BCSR.from_host(sp["M"], sp["K"], sp["bR"], rp, ci, vals, m.DType.F16, device=dev)
+        B = torch.from_numpy(Bf).to(dev).half()
+        C = torch.empty((sp["M"], sp["N"]), dtype=torch.float32, device=dev)
+        probs.append((A, B, C))
+        flops += 2.0 * len(ci) * sp["bR"] * 16 * sp["N"]
+        nbytes += (len(ci) * (sp["bR"] * 32 + 4) + 4 * (sp["M"] // sp["bR"] + 1) +
+                   len(np.unique(ci)) * 16 * sp["N"] * 2 + sp["M"] * sp["N"] * 4)
+    plan = m.BatchPlan(probs)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream())
+    plan.run()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        plan.run()
+
+    def seq():
+        for A, B, C in probs:
+            m.spmm(A, B, C=C)
+
+    g2 = torch.cuda.CUDAGraph()
+    seq()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g2, stream=side):
+        seq()
+
+    def timed(fn):
+        ts = []
+        for k in range(reps + 3):
+            flush.fill_(k & 0xff)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if k >= 3:
+                ts.append(e0.elapsed_time(e1) * 1e3)
+        return float(np.median(ts))
+
+    t_batch = timed(g.replay)
+    t_seq = timed(seq)
+    t_seq_graph = timed(g2.replay)
+    m.device_error_check()
+    plan.close()
+    return {"workload": "64 products, M=K in [512, 8192], bR in {16,32,64}, random/band/blockdiag, "
+                        "density log-uniform [0.5%, 25%], N in {128,256,512}, fp16",
+            "gflop": flops / 1e9, "algorithmic_mb": nbytes / 1e6,
+            "batched_graph_us": t_batch, "sequential_eager_us": t_seq, "sequential_graph_us": t_seq_graph,
+            "speedup_vs_sequential": t_seq / t_batch, "speedup_vs_sequential_graph": t_seq_graph / t_batch,
+            "batched_tflops": flops / (t_batch * 1e-6) / 1e12,
+            "roofline_frac": (nbytes / (t_batch * 1e-6) / 1e9) / hbm_peak}
 
 
 def run_profile(args):
@@ -487,6 +604,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "f16", "bf16", "e4m3", "f16_split"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()

@@ -247,6 +247,9 @@ spmm_status spmm_mlp_adam(float* params, const float* grad, float* m, float* v, 
 typedef struct spmm_cost_model spmm_cost_model;
 spmm_status spmm_cost_model_create(const spmm_mlp_shape* shape, const float* host_params,
                                    spmm_cost_model** out);
+/* The same from a file: "SPMMCM01", int32 in, hidden, layers, out, then the
+ * fp32 parameters (little-endian). */
+spmm_status spmm_cost_model_load(const char* path, spmm_cost_model** out);
 spmm_status spmm_cost_model_destroy(spmm_cost_model* model);
 spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr_desc* A, int N,
                                    spmm_config* out, float* predicted_ms, void* stream);

@@ -1,0 +1,61 @@
+/* Host-side C API of libbcsr_spmm: seeded generators, the .mat text format and
+ * host construction of the BCSR / CSR layouts. No GPU needed; thread-safe.
+ * Errors are reported through spmm_last_error (bcsr_spmm.h). */
+#ifndef BCSR_SPMM_HOST_H
+#define BCSR_SPMM_HOST_H
+#include <stddef.h>
+#include "bcsr_spmm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* mg::generate_matrix<float>(rows, cols, sparsity, pattern, blocksize, seed)
+ * (matrix_generator.cpp:28-140): the same patterns, std::mt19937 stream and
+ * draw order, so the matrix is bit-identical to the reference's. Writes a
+ * row-major fp32 rows x cols buffer; -1 on an unknown pattern. */
+int spmm_generate_matrix(int rows, int cols, double sparsity, const char* pattern, int blocksize,
+                         unsigned seed, float* out);
+
+/* Block structure of an M x K matrix with bR x 16 blocks (no reference
+ * counterpart: the reference's patterns are element patterns).
+ *   pattern 0 random:    each block kept with probability `density`;
+ *   pattern 1 band:      blocks within `param` block columns of the diagonal,
+ *                        each kept with probability min(1, density*KB / band length);
+ *   pattern 2 blockdiag: dense diagonal tiles of `param` x `param` elements;
+ *   pattern 3 lognormal: per-row counts ~ LogNormal(mean density*KB, CV `param`),
+ *                        columns uniform without replacement.
+ * row_ptr holds M/bR + 1 entries, col_idx room for (M/bR) * (K/16). Returns
+ * nnzb, or -1 on bad arguments. */
+long long spmm_gen_structure(int M, int K, int bR, int pattern, double density, double param,
+                             unsigned long long seed, int* row_ptr, int* col_idx);
+
+/* fp32 values of nnzb blocks of bR x bC: dist 0 uniform[-1, 1]; dist 1
+ * N(0,1) x 10^u per block, u ~ uniform[-3, 3]; dist 2 N(0,1). Counter-based,
+ * so the output does not depend on thread count. */
+void spmm_gen_values(long long nnzb, int bR, int bC, int dist, unsigned long long seed, float* out);
+/* `count` dense fp32 values: dist 0 uniform[-1, 1], dist 2 N(0,1). */
+void spmm_gen_dense(long long count, int dist, unsigned long long seed, float* out);
+
+/* The .mat text format (Matrix.cu:14-32; written by matrix_generator.py:110-122):
+ * "rows cols" then rows*cols values, row-major. load rounds to fp16 (bits in
+ * out_half) and counts nonZeros as the reference does. */
+spmm_status spmm_mat_read_header(const char* path, int* rows, int* cols);
+spmm_status spmm_mat_load(const char* path, void* out_half, size_t capacity, int* rows, int* cols,
+                          int* nonZeros);
+spmm_status spmm_mat_save(const char* path, const float* vals, int rows, int cols);
+
+/* BCSRMatrix(matrix, bR, bC) on the host (formats/BCSRMatrix.cu:22-74):
+ * returns nnzb and fills hdr / idx / vals (fp16 bits) when they are non-NULL;
+ * -1 on a block shape the reference rejects. */
+long long spmm_host_dense_to_bcsr(const void* A_half, int rows, int cols, int bR, int bC, int* hdr,
+                                  int* idx, void* vals);
+/* CSRMatrix(matrix) (formats/CSRMatrix.cu:10-43) with the column index of
+ * element i stored as i % cols (the reference stores i). Returns nnz. */
+long long spmm_host_dense_to_csr(const void* A_half, int rows, int cols, int* hdr, int* idx,
+                                 void* vals);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

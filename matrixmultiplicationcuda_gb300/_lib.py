@@ -99,6 +99,7 @@ _SIGS = {
                               c_int, c_vp]),
     "spmm_cost_model_create": (c_int, [ctypes.POINTER(MlpShape), c_vp, ctypes.POINTER(c_vp)]),
     "spmm_cost_model_destroy": (c_int, [c_vp]),
+    "spmm_cost_model_load": (c_int, [c_char_p, ctypes.POINTER(c_vp)]),
     "spmm_cost_model_select": (c_int, [c_vp, ctypes.POINTER(BcsrDesc), c_int, ctypes.POINTER(Config), c_vp,
                                        c_vp]),
     # host side (csrc/host)

@@ -82,5 +82,29 @@ def build(verbose=False):
     return LIB
 
 
+HARNESS = os.path.join(HERE, "harness")
+
+
+def build_tools(verbose=False):
+    """The harness executables (lib/<name>), linked against the library."""
+    build(verbose)
+    out = []
+    for f in sorted(os.listdir(HARNESS)):
+        if not f.endswith(".cu"):
+            continue
+        src = os.path.join(HARNESS, f)
+        exe = os.path.join(OUT, f[:-3])
+        deps = [src, LIB] + [os.path.join(ROOT, "include", h) for h in os.listdir(os.path.join(ROOT, "include"))]
+        if not (os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps)):
+            cmd = [NVCC] + ARCH + ["-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src, "-o", exe + ".tmp",
+                                   "-L" + OUT, "-lbcsr_spmm", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+            os.replace(exe + ".tmp", exe)
+        out.append(exe)
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))

@@ -9,6 +9,7 @@ regret (evaluate()).
 """
 import ctypes
 import math
+import os
 
 import numpy as np
 
@@ -152,8 +153,18 @@ class CostModel:
 
 
 def save(path, s, params, **extra):
+    """npz (shape, params) at `path` and the library's binary format
+    (spmm_cost_model_load) beside it with the extension .bin."""
     np.savez(path, shape=np.array([s.in_, s.hidden, s.layers, s.out], np.int32),
              params=np.asarray(params, np.float32), **extra)
+    save_bin(os.path.splitext(path)[0] + ".bin", s, params)
+
+
+def save_bin(path, s, params):
+    with open(path, "wb") as f:
+        f.write(b"SPMMCM01")
+        f.write(np.array([s.in_, s.hidden, s.layers, s.out], "<i4").tobytes())
+        f.write(np.asarray(params, "<f4").tobytes())
 
 
 # ---- training data: sweeps on seeded synthetic products --------------------------

@@ -16,6 +16,7 @@
 // weight gradients reduce over the batch inside one CTA per output unit, so
 // the gradient is deterministic. Adam updates only the trained range.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 #include "internal.h"
@@ -321,6 +322,28 @@ spmm_status spmm_cost_model_create(const spmm_mlp_shape* shape, const float* hos
   }
   *out = m;
   return SPMM_OK;
+}
+
+spmm_status spmm_cost_model_load(const char* path, spmm_cost_model** out) {
+  if (!path || !out) return fail(SPMM_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(SPMM_ERR_INVALID_ARG, std::string("cannot open ") + path);
+  char magic[8];
+  int32_t dims[4];
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "SPMMCM01", 8) == 0 &&
+            std::fread(dims, sizeof(int32_t), 4, f) == 4;
+  spmm_mlp_shape s{dims[0], dims[1], dims[2], dims[3]};
+  std::vector<float> params;
+  if (ok && valid(&s)) {
+    params.resize((size_t)layout(&s).params());
+    ok = std::fread(params.data(), sizeof(float), params.size(), f) == params.size();
+  } else {
+    ok = false;
+  }
+  std::fclose(f);
+  if (!ok) return fail(SPMM_ERR_INVALID_ARG, std::string("not a cost model file: ") + path);
+  return spmm_cost_model_create(&s, params.data(), out);
 }
 
 spmm_status spmm_cost_model_destroy(spmm_cost_model* m) {

@@ -16,14 +16,19 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def header_functions():
-    text = open(os.path.join(ROOT, "include", "bcsr_spmm.h")).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:spmm_status|int|const char\*)\s+(\w+)\s*\(", text, re.M)))
+    names = set()
+    for h in ("bcsr_spmm.h", "bcsr_spmm_host.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:spmm_status|int|long long|void|const char\*)\s+(\w+)\s*\(", text,
+                                re.M))
+    return sorted(names)
 
 
 def test_library_exports_every_declared_symbol():
     names = header_functions()
     assert "spmm_bcsr_mm" in names and "sparseMatrixMulTensor_launch" in names
+    assert "spmm_gen_values" in names and "spmm_mlp_param_count" in names
     L = ctypes.CDLL(m.lib_path)
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
@@ -182,3 +187,10 @@ int main() {
     hdr, idx, data = oracle.bcsr(A, 32, 16)
     assert (br, bc, nnzb, nz) == (4, 6, len(idx), len(idx) * 512)
     assert csr_nnz == int(np.count_nonzero(A & 0x7fff))
+
+
+def test_harness_built_and_prints_usage():
+    exe = os.path.join(os.path.dirname(m.lib_path), "spmm_nvbench")
+    assert os.path.exists(exe)
+    r = subprocess.run([exe, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "--preset" in r.stderr
