@@ -198,7 +198,7 @@ spmm_status spmm_config_supported(int bR, spmm_dtype dtype, int N, const spmm_co
 /* Exhaustive sweep: times every table entry on this product. Per entry:
  * `warmup` untimed runs, then `reps` runs each preceded (when flush != NULL)
  * by a write of flush_bytes to `flush` (evicting L2) and timed alone with CUDA
- * events; ms_out[i] = the median, +inf where the entry has no kernel.
+ * events; ms_out[i] = the mean, +inf where the entry has no kernel.
  * Overwrites C; synchronises the stream. */
 spmm_status spmm_tune_sweep(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N, float* C, int ldc,
                             int warmup, int reps, void* flush, size_t flush_bytes, float* ms_out,

@@ -123,8 +123,11 @@ spmm_status spmm_tune_sweep(const spmm_bcsr_desc* A, const spmm_dense_desc* B, i
       if (result == SPMM_OK) cudaEventElapsedTime(&ts[k], e0, e1);
     }
     if (result == SPMM_OK) {
-      std::sort(ts.begin(), ts.end());
-      ms_out[i] = ts[reps / 2];
+      // the mean: event timestamps advance in steps of about 2 us on this
+      // hardware, which a median would keep and a mean averages out
+      double sum = 0;
+      for (float x : ts) sum += x;
+      ms_out[i] = (float)(sum / reps);
     }
   }
   cudaEventDestroy(e0);

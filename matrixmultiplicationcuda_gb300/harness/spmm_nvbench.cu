@@ -6,7 +6,9 @@
 // for the library's C ABI: named benches with axes, every state measured on a
 // cold L2 (a 256 MB write before each sample) with CUDA events, samples taken
 // until at least --min-samples and --min-time (or --max-time) are reached,
-// the median reported with its noise (relative standard deviation), and a
+// the mean reported with its noise (relative standard deviation) as NVBench
+// does (the event clock advances in ~2 us steps here, which the mean averages
+// out and a median would not; the median is in the CSV / JSON too), and a
 // post-run check of sampled block rows against an FP64 host product of the
 // values the GPU multiplied. Throughput is TFLOP/s over nonzero-block FLOPs,
 // algorithmic GB/s, and the fraction of the roofline
@@ -390,7 +392,7 @@ void finish_row(Row& r, const DeviceProduct& P, const Peaks& pk) {
   r.nnzb = P.nnzb;
   r.flops = 2.0 * P.nnzb * P.A.bR * 16 * P.N;
   r.bytes = algorithmic_bytes(P);
-  const double t = r.s.median_us * 1e-6;
+  const double t = r.s.mean_us * 1e-6;
   r.tflops = r.flops / t / 1e12;
   r.gbs = r.bytes / t / 1e9;
   const double t_mem = r.bytes / (pk.hbm_gbs * 1e9), t_math = r.flops / (pk.tflops * 1e12);
@@ -513,14 +515,14 @@ class Runner {
     v[2] = {"64 sequential, graph replay", timer_.measure([&] { CK(cudaGraphLaunch(gs, nullptr)); }, o_)};
     SK(spmm_device_error_check(nullptr));
     std::printf("\n## c4: 64 uneven products (%.2f GFLOP, %.1f MB compulsory)\n\n", flops / 1e9, bytes / 1e6);
-    std::printf("| variant | Samples | GPU Time | Noise | TFLOP/s | GB/s | Roofline | vs sequential |\n");
+    std::printf("| variant | Samples | GPU Time (mean) | Noise | TFLOP/s | GB/s | Roofline | vs sequential |\n");
     std::printf("|---|---|---|---|---|---|---|---|\n");
     for (auto& x : v) {
-      const double t = x.s.median_us * 1e-6;
-      std::printf("| %s | %d | %.2f us | %.2f%% | %.1f | %.0f | %.3f | %.2fx |\n", x.name, x.s.samples, x.s.median_us,
+      const double t = x.s.mean_us * 1e-6;
+      std::printf("| %s | %d | %.2f us | %.2f%% | %.1f | %.0f | %.3f | %.2fx |\n", x.name, x.s.samples, x.s.mean_us,
                   100 * x.s.noise, flops / t / 1e12, bytes / t / 1e9, (bytes / (pk_.hbm_gbs * 1e9)) / t,
-                  v[1].s.median_us / x.s.median_us);
-      batch_lines_.push_back({x.name, x.s.median_us, flops, bytes});
+                  v[1].s.mean_us / x.s.mean_us);
+      batch_lines_.push_back({x.name, x.s.mean_us, flops, bytes});
     }
     std::fflush(stdout);
     cudaGraphExecDestroy(gb);
@@ -531,7 +533,7 @@ class Runner {
 
   void header(const char* title) {
     std::printf("\n## %s\n\n", title);
-    std::printf("| M | N | bR | pattern | density | dtype | tuning | config | Samples | GPU Time | Noise | "
+    std::printf("| M | N | bR | pattern | density | dtype | tuning | config | Samples | GPU Time (mean) | Noise | "
                 "TFLOP/s | GB/s | Roofline | bound | max rel err |\n");
     std::printf("|---|---|---|---|---|---|---|---|---|---|---|---|---|---|---|---|\n");
     std::fflush(stdout);
@@ -540,7 +542,7 @@ class Runner {
   void print_row(const Row& r) {
     std::printf("| %d | %d | %d | %s | %.3g | %s | %s | %s | %d | %.2f us | %.2f%% | %.1f | %.0f | %.3f | %s | %.2e |\n",
                 r.spec.M, r.spec.N, r.spec.bR, pattern_name(r.spec.pattern), r.spec.density, dtype_name(r.spec.dtype),
-                r.tuning.c_str(), r.config.c_str(), r.s.samples, r.s.median_us, 100 * r.s.noise, r.tflops, r.gbs,
+                r.tuning.c_str(), r.config.c_str(), r.s.samples, r.s.mean_us, 100 * r.s.noise, r.tflops, r.gbs,
                 r.roof_frac, r.bound.c_str(), r.rel_err);
     std::fflush(stdout);
   }
@@ -549,13 +551,13 @@ class Runner {
     if (!o_.csv.empty()) {
       FILE* f = std::fopen(o_.csv.c_str(), "w");
       if (f) {
-        std::fprintf(f, "bench,M,K,N,bR,pattern,density,dtype,tuning,config,nnzb,samples,median_us,noise,tflops,gbs,"
+        std::fprintf(f, "bench,M,K,N,bR,pattern,density,dtype,tuning,config,nnzb,samples,mean_us,median_us,noise,tflops,gbs,"
                         "roofline_frac,bound,max_rel_err\n");
         for (const Row& r : rows_)
-          std::fprintf(f, "%s,%d,%d,%d,%d,%s,%g,%s,%s,%s,%lld,%d,%.4f,%.5f,%.3f,%.1f,%.4f,%s,%.3e\n", r.spec.bench.c_str(),
-                       r.spec.M, r.spec.K, r.spec.N, r.spec.bR, pattern_name(r.spec.pattern), r.spec.density,
-                       dtype_name(r.spec.dtype), r.tuning.c_str(), r.config.c_str(), r.nnzb, r.s.samples,
-                       r.s.median_us, r.s.noise, r.tflops, r.gbs, r.roof_frac, r.bound.c_str(), r.rel_err);
+          std::fprintf(f, "%s,%d,%d,%d,%d,%s,%g,%s,%s,%s,%lld,%d,%.4f,%.4f,%.5f,%.3f,%.1f,%.4f,%s,%.3e\n",
+                       r.spec.bench.c_str(), r.spec.M, r.spec.K, r.spec.N, r.spec.bR, pattern_name(r.spec.pattern),
+                       r.spec.density, dtype_name(r.spec.dtype), r.tuning.c_str(), r.config.c_str(), r.nnzb,
+                       r.s.samples, r.s.mean_us, r.s.median_us, r.s.noise, r.tflops, r.gbs, r.roof_frac, r.bound.c_str(), r.rel_err);
         std::fclose(f);
       }
     }
@@ -568,17 +570,19 @@ class Runner {
           const Row& r = rows_[i];
           std::fprintf(f,
                        " {\"bench\": \"%s\", \"M\": %d, \"N\": %d, \"bR\": %d, \"pattern\": \"%s\", \"density\": %g, "
-                       "\"dtype\": \"%s\", \"tuning\": \"%s\", \"config\": \"%s\", \"nnzb\": %lld, \"median_us\": %.4f, "
+                       "\"dtype\": \"%s\", \"tuning\": \"%s\", \"config\": \"%s\", \"nnzb\": %lld, \"mean_us\": %.4f, "
+                       "\"median_us\": %.4f, "
                        "\"noise\": %.5f, \"tflops\": %.3f, \"gbs\": %.1f, \"roofline_frac\": %.4f, \"bound\": \"%s\", "
                        "\"max_rel_err\": %.3e}%s\n",
                        r.spec.bench.c_str(), r.spec.M, r.spec.N, r.spec.bR, pattern_name(r.spec.pattern), r.spec.density,
-                       dtype_name(r.spec.dtype), r.tuning.c_str(), r.config.c_str(), r.nnzb, r.s.median_us, r.s.noise,
+                       dtype_name(r.spec.dtype), r.tuning.c_str(), r.config.c_str(), r.nnzb, r.s.mean_us, r.s.median_us,
+                       r.s.noise,
                        r.tflops, r.gbs, r.roof_frac, r.bound.c_str(), std::isnan(r.rel_err) ? -1.0 : r.rel_err,
                        i + 1 < rows_.size() ? "," : "");
         }
         std::fprintf(f, "], \"batched\": [\n");
         for (size_t i = 0; i < batch_lines_.size(); ++i)
-          std::fprintf(f, " {\"variant\": \"%s\", \"median_us\": %.3f, \"gflop\": %.4f, \"mb\": %.2f}%s\n",
+          std::fprintf(f, " {\"variant\": \"%s\", \"mean_us\": %.3f, \"gflop\": %.4f, \"mb\": %.2f}%s\n",
                        batch_lines_[i].name.c_str(), batch_lines_[i].us, batch_lines_[i].flops / 1e9,
                        batch_lines_[i].bytes / 1e6, i + 1 < batch_lines_.size() ? "," : "");
         std::fprintf(f, "]}\n");

@@ -83,7 +83,7 @@ def features(A, N, stream=None):
 
 
 def sweep(A, B, N=None, C=None, warmup=2, reps=5, flush=None, stream=None, B_lo=None):
-    """Median time (ms) of every table entry on C = A @ B; +inf where unsupported."""
+    """Mean time (ms) of every table entry on C = A @ B; +inf where unsupported."""
     import torch
     from .bcsr import _dense_desc
     N = int(B.shape[1]) if N is None else int(N)
