@@ -165,6 +165,12 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
+def whole_job_tflops(flops_per_step, ms_per_step_max, world):
+    """Replicas: every rank runs the same product, so the job's throughput is
+    world x one product's FLOPs over the slowest rank's time per step."""
+    return world * flops_per_step / (ms_per_step_max * 1e-3) / 1e12
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -280,8 +286,33 @@ def reference_wmma_gpu(rp, ci, vals, B, reps=20):
         ts.append(e0.elapsed_time(e1) * 1e3)
     us = float(np.mean(ts))
     flops = 2.0 * len(ci) * BR * 16 * N
-    return {"kernel": "sparseMatrixMulTensor64x16", "us": us, "tflops": flops / (us * 1e-6) / 1e12,
-            "grid": "(N/32, M/64) warps of 32 threads, as the reference harness launches it"}
+    out = {"kernel": "sparseMatrixMulTensor64x16", "us": us, "tflops": flops / (us * 1e-6) / 1e12,
+           "grid": "(N/32, M/64) warps of 32 threads, as the reference harness launches it"}
+    # the 1024^2 16x16 case through the reference's own generator and BCSR build
+    import matrixmultiplicationcuda_gb300 as m
+    A1 = m.generate_matrix(1024, 1024, 0.9, "blockrandom", 16, 123).astype(np.float16)
+    B1 = m.generate_matrix(1024, 1024, 0.0, "random", 16, 456).astype(np.float16)
+    hdr, idx, data = m.host_dense_to_bcsr(A1.view(np.uint16), 16, 16)
+    d1 = [t(hdr), t(idx), t(data.view(np.float16)), t(B1)]
+    C1 = torch.empty((1024, 1024), dtype=torch.float32, device=dev)
+    launch1 = lambda: oracle.ref_wmma_launch("sparseMatrixMulTensor", d1[0].data_ptr(), d1[1].data_ptr(),
+                                             d1[2].data_ptr(), d1[3].data_ptr(), C1.data_ptr(), 1024, 1024, st)
+    for _ in range(3):
+        launch1()
+    ts = []
+    for k in range(reps):
+        flush.fill_(k & 0xff)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch1()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e3)
+    us1 = float(np.mean(ts))
+    f1 = 2.0 * len(idx) * 16 * 16 * 1024
+    return {"A16384_64x16_N512": out,
+            "A1024_16x16_N1024": {"kernel": "sparseMatrixMulTensor", "us": us1, "tflops": f1 / (us1 * 1e-6) / 1e12,
+                                  "nnzb": int(len(idx)), "grid": "(N/16, M/16) warps, as the reference harness"}}
 
 
 def run_ours(args, world, rank, local):
@@ -398,7 +429,7 @@ def run_ours(args, world, rank, local):
     kern_ms = total_ms / args.steps          # average launch duration, launch gaps included
     total_ms = max_over_ranks(total_ms, world)
     ms_step = total_ms / args.steps
-    value = world * flops / (ms_step * 1e-3) / 1e12
+    value = whole_job_tflops(flops, ms_step, world)
 
     # End to end through the public API with host buffers (pinned), tuned precision:
     # every step copies its inputs host -> device, multiplies, and reads C back.
