@@ -13,8 +13,9 @@ Arms:
             scales, split fp16 hi+lo) the learned cost model picks the kernel
             configuration (the exhaustive sweep over the 37 configurations runs
             beside it and is reported as the model's regret); the headline `value`
-            is the fastest precision whose documented error bar
-            (tests/test_gpu_precision.py) is <= 1e-2 relative to FP64. Plain fp16
+            is the fastest precision whose measured error on this workload
+            (max-relative against an FP64 product of the fp32 inputs, on sampled
+            block rows) is <= 1e-2. Plain fp16
             (the library's default configuration, no tuning) is reported beside it.
             The line also carries the batched workload: 64 uneven products in one
             persistent launch replayed from a CUDA graph, against 64 sequential
@@ -63,6 +64,19 @@ def make_structure():
     import matrixmultiplicationcuda_gb300 as m
     rp, ci = m.gen_structure(M, K, BR, m.PATTERN_RANDOM, DENSITY, 0, seed=SEED)
     return rp, ci
+
+
+def fp64_rows(rp, ci, vals, Bf, rows):
+    """FP64 product of block rows `rows` of A (fp32 block values) and B (fp32)."""
+    blocks = vals.reshape(-1, BR, 16).astype(np.float64)
+    Bd = Bf.astype(np.float64)
+    out = []
+    for r in rows:
+        acc = np.zeros((BR, N))
+        for k in range(rp[r], rp[r + 1]):
+            acc += blocks[k] @ Bd[ci[k] * 16:(ci[k] + 1) * 16]
+        out.append(acc)
+    return np.concatenate(out)
 
 
 def work_units(rp, ci):
@@ -399,10 +413,24 @@ def run_ours(args, world, rank, local):
                          "sweep_ms": t_sweep, "sweep_cfg": cfg_sweep,
                          "err_bar": ERROR_BAR[name], "bytes": algorithmic_bytes(nnzb, cols_touched, name)}
     model.close()
+    # error of every precision against an FP64 product of the exact fp32 inputs,
+    # on sampled block rows
+    sample_rows = [0, (M // BR) // 3, 2 * (M // BR) // 3, M // BR - 1]
+    ref = fp64_rows(rp, ci, vals, Bf, sample_rows)
+    for name in results:
+        A0, Bq0, Blo0, bs0, C0 = prepared[name][0]
+        launch(prepared[name][0], results[name]["cfg"])
+        torch.cuda.synchronize()
+        got = np.concatenate([C0[r * BR:(r + 1) * BR].cpu().numpy() for r in sample_rows])
+        d = got.astype(np.float64) - ref
+        results[name]["max_rel"] = float(np.abs(d).max() / np.abs(ref).max())
+        results[name]["fro_rel"] = float(np.linalg.norm(d) / np.linalg.norm(ref))
     # plain fp16: the library's default configuration, no tuning
     time_loop(prepared["f16"], None, 3)
     plain_ms = time_loop(prepared["f16"], None, 30)
-    ok = {k: v for k, v in results.items() if v["err_bar"] <= TARGET_ERR}
+    # the headline precision: the fastest whose measured error on this workload
+    # is within the target (max-relative against FP64)
+    ok = {k: v for k, v in results.items() if v["max_rel"] <= TARGET_ERR} or {"f16": results["f16"]}
     tuned = min(ok, key=lambda k: results[k]["ms"])
     probs, cfg = prepared[tuned], results[tuned]["cfg"]
 
@@ -519,8 +547,10 @@ def run_ours(args, world, rank, local):
             "precisions": {k: {"tflops": v["tflops"], "ms": v["ms"], "err_bar": v["err_bar"],
                                "model_pick": tuner.config_name(v["cfg"]),
                                "sweep_best": tuner.config_name(v["sweep_cfg"]), "sweep_best_ms": v["sweep_ms"],
-                               "model_regret": v["ms"] / v["sweep_ms"] - 1.0}
+                               "model_regret": v["ms"] / v["sweep_ms"] - 1.0,
+                               "max_rel_err": v["max_rel"], "fro_rel_err": v["fro_rel"]}
                            for k, v in results.items()},
+            "error_sample": "block rows %s, against an FP64 product of the fp32 inputs" % sample_rows,
             "batched": batched,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 #include "internal.h"
 
 namespace spmm {
@@ -48,6 +49,66 @@ int sm_count() {
   return g_sms[d];
 }
 
+int smem_per_sm() {
+  static int cache[kMaxDevices] = {0};
+  int d = current_device();
+  if (d < 0 || d >= kMaxDevices) return 0;
+  if (cache[d] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerMultiprocessor, d);
+    cache[d] = n;
+  }
+  return cache[d];
+}
+
+namespace {
+// Per-device caches of kernel attributes (keyed by kernel address).
+struct FnKey {
+  const void* fn;
+  int dev, a, b;
+  bool operator==(const FnKey& o) const { return fn == o.fn && dev == o.dev && a == o.a && b == o.b; }
+};
+struct FnVal {
+  FnKey k;
+  int v;
+};
+std::vector<FnVal> g_fn_cache;
+}  // namespace
+
+cudaError_t ensure_smem_attr(const void* fn, int bytes) {
+  const FnKey k{fn, current_device(), bytes, -1};
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (const FnVal& e : g_fn_cache)
+      if (e.k == k) return cudaSuccess;
+  }
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_fn_cache.push_back({k, 1});
+  }
+  return e;
+}
+
+int max_blocks_per_sm(const void* fn, int threads, size_t smem) {
+  const FnKey k{fn, current_device(), threads, (int)smem};
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (const FnVal& e : g_fn_cache)
+      if (e.k == k) return e.v;
+  }
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) n = 1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_fn_cache.push_back({k, n});
+  return n;
+}
+
+bool pdl_enabled() {
+  static const bool on = std::getenv("SPMM_NO_PDL") == nullptr;
+  return on;
+}
+
 unsigned* device_error_word() {
   int d = current_device();
   if (d < 0 || d >= kMaxDevices) return nullptr;
@@ -90,9 +151,67 @@ unsigned long long wait_limit_ns() {
   return v;
 }
 
+namespace {
+// Encoded tensor maps, reused across calls: an encoding depends only on its
+// arguments, and repeated products on the same buffers are the common case.
+struct MapKey {
+  int rank, dt, swz;
+  const void* base;
+  uint64_t d0, d1, d2, s0, s1;
+  uint32_t b0, b1, b2;
+  bool operator==(const MapKey& o) const { return std::memcmp(this, &o, sizeof(MapKey)) == 0; }
+};
+struct MapEntry {
+  MapKey k;
+  CUtensorMap map;
+};
+constexpr int kMapCache = 128;
+MapEntry g_maps[kMapCache];
+int g_maps_used = 0, g_maps_next = 0;
+
+bool map_lookup(const MapKey& k, CUtensorMap* out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (int i = 0; i < g_maps_used; ++i)
+    if (g_maps[i].k == k) {
+      *out = g_maps[i].map;
+      return true;
+    }
+  return false;
+}
+void map_store(const MapKey& k, const CUtensorMap& m) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  MapEntry& e = g_maps[g_maps_next];
+  e.k = k;
+  e.map = m;
+  g_maps_next = (g_maps_next + 1) % kMapCache;
+  if (g_maps_used < kMapCache) ++g_maps_used;
+}
+MapKey map_key(int rank, int dt, int swz, const void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s0,
+               uint64_t s1, uint32_t b0, uint32_t b1, uint32_t b2) {
+  MapKey k;
+  std::memset(&k, 0, sizeof(k));   // padding takes part in the comparison
+  k.rank = rank;
+  k.dt = dt;
+  k.swz = swz;
+  k.base = base;
+  k.d0 = d0;
+  k.d1 = d1;
+  k.d2 = d2;
+  k.s0 = s0;
+  k.s1 = s1;
+  k.b0 = b0;
+  k.b1 = b1;
+  k.b2 = b2;
+  return k;
+}
+}  // namespace
+
 spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const void* base,
                                uint64_t inner, uint64_t outer, uint64_t row_stride_bytes,
                                uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz) {
+  const MapKey key = map_key(2, (int)dt, (int)swz, base, inner, outer, 0, row_stride_bytes, 0, box_inner,
+                             box_outer, 0);
+  if (map_lookup(key, map)) return SPMM_OK;
   {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_encode) {
@@ -116,12 +235,16 @@ spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const v
     return fail(SPMM_ERR_INVALID_ARG,
                 "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) +
                     "): B needs a 16-byte aligned base and a row stride that is a multiple of 16 bytes");
+  map_store(key, *map);
   return SPMM_OK;
 }
 
 spmm_status encode_panel_map_3d(CUtensorMap* map, const void* base, uint64_t N, uint64_t K,
                                 uint64_t row_stride_bytes, uint32_t boxes) {
   if (N % 64 || boxes == 0 || boxes > 256) return fail(SPMM_ERR_UNSUPPORTED, "panel map needs N % 64 == 0");
+  const MapKey key = map_key(3, (int)CU_TENSOR_MAP_DATA_TYPE_UINT16, (int)CU_TENSOR_MAP_SWIZZLE_128B, base, 64, K,
+                             N / 64, row_stride_bytes, 128, 64, 16, boxes);
+  if (map_lookup(key, map)) return SPMM_OK;
   CUtensorMap probe;
   spmm_status st = encode_tile_map_2d(&probe, CU_TENSOR_MAP_DATA_TYPE_UINT16, base, N, K, row_stride_bytes,
                                       64, 16, CU_TENSOR_MAP_SWIZZLE_128B);   // resolves the entry point
@@ -135,6 +258,7 @@ spmm_status encode_panel_map_3d(CUtensorMap* map, const void* base, uint64_t N, 
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     return fail(SPMM_ERR_UNSUPPORTED, "3-D panel tensor map rejected (" + std::to_string((int)r) + ")");
+  map_store(key, *map);
   return SPMM_OK;
 }
 

@@ -18,6 +18,31 @@ spmm_status cuda_fail(cudaError_t e, const char* what);
   } while (0)
 
 int sm_count();                                  // SMs of the current device
+int smem_per_sm();                               // shared memory per SM of the current device (bytes)
+// Sets a kernel's dynamic shared-memory limit once per device (cached).
+cudaError_t ensure_smem_attr(const void* fn, int bytes);
+// Occupancy query, cached per (kernel, device, block, smem).
+int max_blocks_per_sm(const void* fn, int threads, size_t smem);
+
+// Programmatic dependent launch (on unless SPMM_NO_PDL is set): the library's
+// pipeline kernels wait (griddepcontrol.wait) before touching global memory,
+// so they may start while the previous kernel in the stream finishes.
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+cudaError_t launch_kernel(void (*fn)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                          Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, static_cast<Args&&>(args)...);
+}
 unsigned* device_error_word();                   // per-device error word (lazy)
 // A zeroed pair {next item, CTAs done} for one persistent launch's work queue.
 // Slots rotate over a per-device pool; each launch's last CTA zeroes its slot

@@ -59,6 +59,20 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_
   return true;
 }
 
+// ---- programmatic dependent launch ---------------------------------------------
+// A kernel launched with programmatic stream serialisation may start while the
+// previous kernel in the stream is still running. It signals early that its
+// own successor may start (launch_dependents: the successor's CTAs are placed
+// as this grid's CTAs leave their SMs) and, before it touches global memory,
+// waits until every prerequisite grid has completed and its writes are
+// visible (wait). Everything before the wait -- barrier setup, TMEM
+// allocation, tensor-map prefetch from parameter space -- overlaps the
+// previous kernel's tail.
+__device__ __forceinline__ void grid_dep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---- TMA -----------------------------------------------------------------------
 // Untiled bulk copy global -> shared (16-byte aligned ends, size % 16 == 0).
 __device__ __forceinline__ void tma_bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,

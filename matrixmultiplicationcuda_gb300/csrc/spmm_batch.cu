@@ -130,6 +130,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  grid_dep_launch_dependents();
+  grid_dep_wait();
 
   // Ring entry `it`, read by a whole warp: lane 0 waits (bounded), every lane
   // copies the record, lane 0 releases the entry. False on a timeout.
@@ -627,8 +629,8 @@ spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream) {
   p.queue = plan->d_queue;
   p.err = plan->err;
   p.timeout_ns = plan->timeout_ns;
-  plan->entry->fn<<<(unsigned)plan->grid, kBatchThreads, plan->entry->smem, static_cast<cudaStream_t>(stream)>>>(p);
-  SPMM_CUDA_TRY(cudaGetLastError());
+  SPMM_CUDA_TRY(launch_kernel(plan->entry->fn, dim3((unsigned)plan->grid), dim3(kBatchThreads), plan->entry->smem,
+                              static_cast<cudaStream_t>(stream), p));
   return SPMM_OK;
 }
 

@@ -152,12 +152,10 @@ spmm_status launch_mma(const LaunchRequest& r) {
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
 
-  SPMM_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(e->fn),
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
+  SPMM_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(e->fn), (int)e->smem));
   int per_sm = r.cfg.ctas_per_sm;
   if (per_sm <= 0) {
-    SPMM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, reinterpret_cast<const void*>(e->fn), e->threads, e->smem));
+    per_sm = max_blocks_per_sm(reinterpret_cast<const void*>(e->fn), e->threads, e->smem);
     if (per_sm < 1) per_sm = 1;
   }
   long long grid = (long long)sm_count() * per_sm;
@@ -165,8 +163,7 @@ spmm_status launch_mma(const LaunchRequest& r) {
   if (std::getenv("SPMM_DEBUG"))
     std::fprintf(stderr, "[spmm] mma.sync bR=%d nt=%d stages=%d smem=%zu per_sm=%d grid=%lld items=%d\n",
                  A.bR, nt, e->stages, e->smem, per_sm, grid, p.n_items);
-  e->fn<<<(unsigned)grid, e->threads, e->smem, r.stream>>>(tmB, tmBlo, p);
-  SPMM_CUDA_TRY(cudaGetLastError());
+  SPMM_CUDA_TRY(launch_kernel(e->fn, dim3((unsigned)grid), dim3(e->threads), e->smem, r.stream, tmB, tmBlo, p));
   return SPMM_OK;
 }
 

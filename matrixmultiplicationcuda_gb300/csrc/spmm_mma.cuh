@@ -93,6 +93,8 @@ __global__ void __launch_bounds__(MmaCfg<BR, NT, WM, WN, STAGES, MODE>::kThreads
     fence_mbar_init();
   }
   __syncthreads();
+  grid_dep_launch_dependents();
+  grid_dep_wait();
 
   if (warp == Cfg::kConsumerWarps) {
     // ------------------------------ producer warp ------------------------------

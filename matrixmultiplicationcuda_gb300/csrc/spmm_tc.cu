@@ -140,6 +140,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  grid_dep_launch_dependents();
+  grid_dep_wait();
 
   // Ring entry `it` of the item stream (bounded wait); *item < 0 ends the stream.
   auto read_item = [&](uint32_t it, int* item, int* start, int* end, unsigned code) -> bool {
@@ -559,15 +561,12 @@ spmm_status launch_tc(const LaunchRequest& r) {
   if (p.n_items == 0) return SPMM_OK;
   if (p.split > 1)
     SPMM_CUDA_TRY(cudaMemset2DAsync(r.C, (size_t)r.ldc * 4, 0, (size_t)r.N * 4, A.M, r.stream));
-  SPMM_CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(e->fn),
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
+  SPMM_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(e->fn), (int)e->smem));
   // CTAs per SM from the real limits: TMEM columns (512 per SM), shared memory
   // per SM, and the two CTAs the launch bounds budget registers for. (The
   // runtime's occupancy query reports one CTA per SM for this kernel, while two
   // run side by side.)
-  int dev = 0, smem_sm = 0;
-  SPMM_CUDA_TRY(cudaGetDevice(&dev));
-  SPMM_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  const int smem_sm = smem_per_sm();
   const int tmem_fit = 512 / e->tmem_cols;
   const int smem_fit = smem_sm / (int)(e->smem + 1024);
   int per_sm = std::min(2, std::min(tmem_fit, smem_fit));
@@ -581,8 +580,8 @@ spmm_status launch_tc(const LaunchRequest& r) {
                  "items=%d panel3d=%d queue=%d split=%d\n",
                  A.bR, nt, e->stages, e->acc, e->group, e->smem, e->tmem_cols, per_sm, grid, p.n_items, panel3d,
                  p.queue != nullptr, p.split);
-  e->fn<<<(unsigned)grid, kTcThreads, e->smem, r.stream>>>(tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo, p);
-  SPMM_CUDA_TRY(cudaGetLastError());
+  SPMM_CUDA_TRY(launch_kernel(e->fn, dim3((unsigned)grid), dim3(kTcThreads), e->smem, r.stream, tmA1, tmAg, tmAlo1,
+                              tmAlog, tmB, tmBlo, p));
   return SPMM_OK;
 }
 

@@ -14,7 +14,7 @@
 // algorithmic GB/s, and the fraction of the roofline
 //   t_roof = max(FLOPs / tensor peak, compulsory bytes / HBM peak).
 //
-//   spmm_nvbench [--preset c1|c2|c3|c4|all] [--tuning default,model,sweep]
+//   spmm_nvbench [--preset c1|c2|c3|c4|launch|all] [--tuning default,model,sweep]
 //                [--min-samples 20] [--min-time 0.2] [--max-time 2]
 //                [--csv FILE] [--json FILE] [--model FILE] [--peaks FILE]
 //                [--filter SUBSTRING] [--no-check]
@@ -33,6 +33,8 @@
 //       random / band / block-diagonal, density log-uniform 0.5-25 %, N in
 //       {128, 256, 512}): one persistent launch replayed from a CUDA graph
 //       against 64 sequential launches, eager and graph-captured.
+//   launch  host time per call and back-to-back launch rate (L2 warm) on the
+//       c1 and c3 products (not part of "all").
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
@@ -40,6 +42,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -531,6 +534,33 @@ class Runner {
     spmm_batch_plan_destroy(plan);
   }
 
+  // Host time per call and back-to-back launch rate (L2 warm: the same buffers
+  // every launch; consecutive launches may overlap through programmatic
+  // dependent launch unless SPMM_NO_PDL is set).
+  void launch_bench(const Spec& spec, const char* label) {
+    DeviceProduct P;
+    build_product(spec, P);
+    constexpr int kCalls = 200;
+    for (int i = 0; i < 20; ++i) SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, nullptr, nullptr));
+    CK(cudaDeviceSynchronize());
+    double host_us = 1e30, gpu_us = 1e30;
+    for (int rep = 0; rep < 5; ++rep) {
+      CK(cudaEventRecord(timer_.e0, nullptr));
+      const auto t0 = std::chrono::steady_clock::now();
+      for (int i = 0; i < kCalls; ++i) SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, nullptr, nullptr));
+      const auto t1 = std::chrono::steady_clock::now();
+      CK(cudaEventRecord(timer_.e1, nullptr));
+      CK(cudaEventSynchronize(timer_.e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, timer_.e0, timer_.e1));
+      host_us = std::min(host_us, std::chrono::duration<double, std::micro>(t1 - t0).count() / kCalls);
+      gpu_us = std::min(gpu_us, ms * 1e3 / kCalls);
+    }
+    std::printf("| %s | %s | %.2f us | %.2f us | %.1f |\n", label, std::getenv("SPMM_NO_PDL") ? "off" : "on", host_us,
+                gpu_us, 2.0 * P.nnzb * P.A.bR * 16 * P.N / (gpu_us * 1e-6) / 1e12);
+    std::fflush(stdout);
+  }
+
   void header(const char* title) {
     std::printf("\n## %s\n\n", title);
     std::printf("| M | N | bR | pattern | density | dtype | tuning | config | Samples | GPU Time (mean) | Noise | "
@@ -689,6 +719,12 @@ int main(int argc, char** argv) {
       }
     } else if (p == "c4") {
       run.batched_bench();
+    } else if (p == "launch") {
+      std::printf("\n## launch: host time per spmm_bcsr_mm call, back-to-back launches (L2 warm)\n\n");
+      std::printf("| product | PDL | host per call | GPU per launch | TFLOP/s |\n|---|---|---|---|---|\n");
+      run.launch_bench(Spec{"launch", 1024, 1024, 1024, 16, 4, 0.10, 0.0, 0, 0, SPMM_F16, 123}, "1024^2 16x16 10%, N 1024");
+      run.launch_bench(Spec{"launch", 16384, 16384, 512, 64, 0, 0.02, 0.0, 1, 2, SPMM_F16, 20240},
+                       "16384^2 64x16 2%, N 512");
     } else {
       std::fprintf(stderr, "unknown preset %s\n", p.c_str());
       return 1;
