@@ -45,7 +45,8 @@ typedef enum spmm_dtype {
 
 /* Kernel configuration. Zero-initialised = let the library choose. */
 typedef struct spmm_config {
-  int kernel;    /* 0 = auto, 1 = mma.sync pipeline, 2 = tcgen05 pipeline              */
+  int kernel;    /* 0 = auto, 1 = mma.sync pipeline, 2 = tcgen05 pipeline,
+                    3 = tcgen05 pipeline for 64-row blocks with M = 64 UMMAs       */
   int n_tile;    /* output columns per CTA tile: 64, 128 or 256 (0 = auto)           */
   int stages;    /* pipeline depth 2..8 (0 = auto)                                   */
   int ctas_per_sm; /* persistent grid = SMs x this (0 = auto)                          */
@@ -185,9 +186,10 @@ spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
 /* ---- tuning ----------------------------------------------------------------------
  * No counterpart in the reference (its harness sweeps kernels by hand).
  * The configuration space: a fixed table of spmm_tune_config_count() entries
- * (37: five mma.sync column tiles and depths; tcgen05 column tiles, depths,
- * accumulator counts, static or work-queue schedules and split-K). Not every
- * entry has a kernel for every block height and type. */
+ * (41: five mma.sync column tiles and depths; tcgen05 column tiles, depths,
+ * accumulator counts, static or work-queue schedules and split-K; the 64-row
+ * tcgen05 pipeline's column tiles and schedules). Not every entry has a kernel
+ * for every block height and type. */
 int spmm_tune_config_count(void);
 spmm_status spmm_tune_config(int i, spmm_config* out);
 /* The configuration spmm_bcsr_mm runs when given none (the library's fixed

@@ -50,10 +50,15 @@ __global__ void __launch_bounds__(kConvThreads)
     const int sub = lane % lpb;
     bool nz = false;
     if (j < KB) {
+      // eight rows per step, all loads in flight before the test (a test per
+      // row would serialise the loads of an all-zero block)
       const uint16_t* p = arow + (long long)j * bC + sub * 8;
-      for (int x = 0; x < bR && !nz; ++x) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(p + (long long)x * lda));
-        nz = any_nonzero_h8(v);
+      for (int x0 = 0; x0 < bR && !nz; x0 += 8) {
+        uint4 v[8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) v[x] = __ldg(reinterpret_cast<const uint4*>(p + (long long)(x0 + x) * lda));
+#pragma unroll
+        for (int x = 0; x < 8; ++x) nz = nz || any_nonzero_h8(v[x]);
       }
     }
     const uint32_t bal = __ballot_sync(0xffffffffu, nz);
@@ -158,44 +163,83 @@ __global__ void k_validate_cols(const int* row_ptr, const int* col_idx, int MB, 
 }
 
 // ---- precision conversion -------------------------------------------------------
-__global__ void k_to_f16(const float* src, size_t n, __half* dst, __half* lo) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
+// Conversions read 16 bytes (four values) per thread per step when every
+// pointer allows it (vec != 0), then finish the last n % 4 values one by one.
+__device__ __forceinline__ uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+
+__global__ void k_to_f16(const float* src, size_t n, __half* dst, __half* lo, int vec) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t n4 = vec ? n / 4 : 0;
+  for (size_t q = t; q < n4; q += stride) {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(src) + q);
+    const __half2 a = __floats2half2_rn(x.x, x.y), b = __floats2half2_rn(x.z, x.w);
+    reinterpret_cast<uint2*>(dst)[q] = make_uint2(h2_bits(a), h2_bits(b));
+    if (lo) {
+      const float2 fa = __half22float2(a), fb = __half22float2(b);
+      const __half2 la = __floats2half2_rn(x.x - fa.x, x.y - fa.y), lb = __floats2half2_rn(x.z - fb.x, x.w - fb.y);
+      reinterpret_cast<uint2*>(lo)[q] = make_uint2(h2_bits(la), h2_bits(lb));
+    }
+  }
+  for (size_t i = n4 * 4 + t; i < n; i += stride) {
     const float x = src[i];
     const __half h = __float2half_rn(x);
     dst[i] = h;
     if (lo) lo[i] = __float2half_rn(x - __half2float(h));
   }
 }
-__global__ void k_to_bf16(const float* src, size_t n, __nv_bfloat16* dst) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = __float2bfloat16_rn(src[i]);
-}
-// Per-block absolute maximum into scales[] (as ordered uint bits, scales zeroed first).
-__global__ void k_absmax(const float* src, size_t n, int block_elems, unsigned* smax) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const float a = fabsf(src[i]);
-    if (a > 0.f) atomicMax(smax + i / block_elems, __float_as_uint(a));
+__global__ void k_to_bf16(const float* src, size_t n, __nv_bfloat16* dst, int vec) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t n4 = vec ? n / 4 : 0;
+  for (size_t q = t; q < n4; q += stride) {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(src) + q);
+    __nv_bfloat162 a = __floats2bfloat162_rn(x.x, x.y), b = __floats2bfloat162_rn(x.z, x.w);
+    reinterpret_cast<uint2*>(dst)[q] =
+        make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
   }
+  for (size_t i = n4 * 4 + t; i < n; i += stride) dst[i] = __float2bfloat16_rn(src[i]);
 }
-// One CTA per scale block when blocks are small: reduction in shared memory.
-__global__ void k_absmax_small(const float* src, size_t n, int block_elems, float* scales) {
+// Absolute maximum of large scale blocks: CTA (x, y) reduces chunk x of scale
+// block y and merges it with one atomicMax (ordered uint bits; scales zeroed first).
+constexpr int kAbsChunk = 256 * 16;
+__global__ void k_absmax(const float* src, size_t n, int block_elems, unsigned* smax) {
   __shared__ float red[32];
-  const size_t b = blockIdx.x;
-  const size_t lo = b * (size_t)block_elems;
+  const size_t blo = (size_t)blockIdx.y * block_elems;
+  const size_t lo = blo + (size_t)blockIdx.x * kAbsChunk;
+  const size_t hi = min(min(lo + (size_t)kAbsChunk, blo + (size_t)block_elems), n);
   float m = 0.f;
-  for (size_t i = lo + threadIdx.x; i < lo + block_elems && i < n; i += blockDim.x)
-    m = fmaxf(m, fabsf(src[i]));
+  for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) m = fmaxf(m, fabsf(src[i]));
   for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
     m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
     for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (threadIdx.x == 0) scales[b] = m;
+    if (threadIdx.x == 0 && m > 0.f) atomicMax(smax + blockIdx.y, __float_as_uint(m));
   }
+}
+// One warp per scale block when blocks are small (<= 8192 elements): 16-byte
+// loads when the block starts 16-byte aligned (vec), a shuffle reduction.
+__global__ void k_absmax_small(const float* src, size_t n, int block_elems, float* scales, size_t nblocks,
+                               int vec) {
+  const size_t b = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= nblocks) return;
+  const size_t lo = b * (size_t)block_elems;
+  const size_t hi = min(lo + (size_t)block_elems, n);
+  float m = 0.f;
+  if (vec && hi - lo == (size_t)block_elems) {
+    const float4* p = reinterpret_cast<const float4*>(src + lo);
+    for (int q = lane; q < block_elems / 4; q += 32) {
+      const float4 x = __ldg(p + q);
+      m = fmaxf(m, fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fmaxf(fabsf(x.z), fabsf(x.w))));
+    }
+  } else {
+    for (size_t i = lo + lane; i < hi; i += 32) m = fmaxf(m, fabsf(src[i]));
+  }
+  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) scales[b] = m;
 }
 // max -> scale: max / 448 (the largest finite e4m3), 1 for an all-zero block.
 __global__ void k_finish_scales(float* scales, size_t nblocks) {
@@ -206,9 +250,21 @@ __global__ void k_finish_scales(float* scales, size_t nblocks) {
   }
 }
 __global__ void k_to_e4m3(const float* src, size_t n, int block_elems, const float* scales,
-                          __nv_fp8_storage_t* dst) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
+                          __nv_fp8_storage_t* dst, int vec) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t n4 = vec ? n / 4 : 0;
+  // vec is set only when block_elems % 4 == 0: the four values share a scale
+  for (size_t q = t; q < n4; q += stride) {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(src) + q);
+    const float sc = scales[(q * 4) / (size_t)block_elems];
+    const uint32_t packed = (uint32_t)__nv_cvt_float_to_fp8(x.x / sc, __NV_SATFINITE, __NV_E4M3) |
+                            (uint32_t)__nv_cvt_float_to_fp8(x.y / sc, __NV_SATFINITE, __NV_E4M3) << 8 |
+                            (uint32_t)__nv_cvt_float_to_fp8(x.z / sc, __NV_SATFINITE, __NV_E4M3) << 16 |
+                            (uint32_t)__nv_cvt_float_to_fp8(x.w / sc, __NV_SATFINITE, __NV_E4M3) << 24;
+    reinterpret_cast<uint32_t*>(dst)[q] = packed;
+  }
+  for (size_t i = n4 * 4 + t; i < n; i += stride)
     dst[i] = __nv_cvt_float_to_fp8(src[i] / scales[i / block_elems], __NV_SATFINITE, __NV_E4M3);
 }
 
@@ -331,32 +387,37 @@ spmm_status spmm_quantize(const float* src, size_t count, spmm_dtype dtype, int 
   if (count == 0) return SPMM_OK;
   if (!src || !dst) return fail(SPMM_ERR_INVALID_ARG, "null pointer");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const unsigned g = grid_for(count);
+  const unsigned g = grid_for((count + 3) / 4);
+  auto al = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; };
+  const int vec2 = al(src, 16) && al(dst, 8) && (!dst_lo || al(dst_lo, 8)) ? 1 : 0;
   switch (dtype) {
     case SPMM_F16:
-      k_to_f16<<<g, 256, 0, s>>>(src, count, static_cast<__half*>(dst), nullptr);
+      k_to_f16<<<g, 256, 0, s>>>(src, count, static_cast<__half*>(dst), nullptr, vec2);
       break;
     case SPMM_F16_SPLIT:
       if (!dst_lo) return fail(SPMM_ERR_INVALID_ARG, "F16_SPLIT needs dst_lo");
-      k_to_f16<<<g, 256, 0, s>>>(src, count, static_cast<__half*>(dst), static_cast<__half*>(dst_lo));
+      k_to_f16<<<g, 256, 0, s>>>(src, count, static_cast<__half*>(dst), static_cast<__half*>(dst_lo), vec2);
       break;
     case SPMM_BF16:
-      k_to_bf16<<<g, 256, 0, s>>>(src, count, static_cast<__nv_bfloat16*>(dst));
+      k_to_bf16<<<g, 256, 0, s>>>(src, count, static_cast<__nv_bfloat16*>(dst), vec2);
       break;
     case SPMM_E4M3: {
       if (!scales || block_elems <= 0) return fail(SPMM_ERR_INVALID_ARG, "E4M3 needs scales and block_elems");
       const size_t nblocks = (count + block_elems - 1) / block_elems;
       if (block_elems <= 8192) {
-        k_absmax_small<<<(unsigned)nblocks, 256, 0, s>>>(src, count, block_elems, scales);
+        const int vec = al(src, 16) && block_elems % 4 == 0 ? 1 : 0;
+        k_absmax_small<<<(unsigned)((nblocks + 7) / 8), 256, 0, s>>>(src, count, block_elems, scales, nblocks, vec);
       } else {
         SPMM_CUDA_TRY(cudaMemsetAsync(scales, 0, nblocks * sizeof(float), s));
-        k_absmax<<<g, 256, 0, s>>>(src, count, block_elems, reinterpret_cast<unsigned*>(scales));
+        if (nblocks > 65535) return fail(SPMM_ERR_UNSUPPORTED, "too many large scale blocks");
+        const dim3 ag((unsigned)((block_elems + kAbsChunk - 1) / kAbsChunk), (unsigned)nblocks);
+        k_absmax<<<ag, 256, 0, s>>>(src, count, block_elems, reinterpret_cast<unsigned*>(scales));
       }
       SPMM_CUDA_TRY(cudaGetLastError());
       k_finish_scales<<<grid_for(nblocks), 256, 0, s>>>(scales, nblocks);
       SPMM_CUDA_TRY(cudaGetLastError());
-      k_to_e4m3<<<g, 256, 0, s>>>(src, count, block_elems, scales,
-                                  static_cast<__nv_fp8_storage_t*>(dst));
+      k_to_e4m3<<<g, 256, 0, s>>>(src, count, block_elems, scales, static_cast<__nv_fp8_storage_t*>(dst),
+                                  al(src, 16) && al(dst, 4) && block_elems % 4 == 0 ? 1 : 0);
       break;
     }
     default:

@@ -328,6 +328,7 @@ spmm_status spmm_bcsr_mm(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int 
   std::memset(&r.cfg, 0, sizeof(r.cfg));
   if (cfg) r.cfg = *cfg;
   r.stream = static_cast<cudaStream_t>(stream);
+  if (r.cfg.kernel == 3) return launch_tc64(r);
   if (r.cfg.kernel == 2 || (r.cfg.kernel == 0 && A->bR == 64)) {
     spmm_status st = launch_tc(r);
     if (st != SPMM_ERR_UNSUPPORTED || r.cfg.kernel == 2) return st;

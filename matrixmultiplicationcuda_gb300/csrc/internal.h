@@ -79,11 +79,14 @@ struct LaunchRequest {
 spmm_status launch_mma(const LaunchRequest& r);
 // tcgen05 family (spmm_tc.cu); returns SPMM_ERR_UNSUPPORTED when it has no kernel for r
 spmm_status launch_tc(const LaunchRequest& r);
+// tcgen05, 64-row blocks, M = 64 UMMAs (spmm_tc64.cu)
+spmm_status launch_tc64(const LaunchRequest& r);
 
 // Whether a pipeline has an instantiation for this block height, type, N and
 // configuration (the same lookup its launcher makes).
 bool mma_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg);
 bool tc_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg);
+bool tc64_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg);
 int mma_default_nt(int bR, spmm_dtype dtype, int N);   // the column tile spmm_bcsr_mm picks by default
 
 unsigned long long wait_limit_ns();              // bounded-wait limit for device waits

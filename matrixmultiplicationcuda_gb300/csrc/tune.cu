@@ -1,11 +1,12 @@
 // The tuner's configuration space, the exhaustive sweep over it, and the
 // device-array wrapper of the structure features.
 //
-// The table has 37 entries: five mma.sync tiles (column tile x ring depth)
-// and 32 tcgen05 variants (column tile, ring depth, TMEM accumulators, static
-// or work-queue schedule, split-K of 1, 2, 4 and, for the default 256-column
-// tile, 8). Which entries have a kernel depends on the block height and the
-// type; spmm_config_supported answers that without launching.
+// The table has 41 entries: five mma.sync tiles (column tile x ring depth),
+// 32 variants of the 128-column tcgen05 pipeline (column tile, ring depth,
+// TMEM accumulators, static or work-queue schedule, split-K of 1, 2, 4 and,
+// for the default 256-column tile, 8) and four of the 64-row pipeline (column
+// tile x schedule). Which entries have a kernel depends on the block height
+// and the type; spmm_config_supported answers that without launching.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -40,6 +41,9 @@ std::vector<spmm_config> make_table() {
   for (const Tc& x : tcs)
     for (int sched = 0; sched < 2; ++sched)
       for (int split = 1; split <= x.max_split; split *= 2) add(2, x.nt, x.stages, x.acc, sched, split);
+  // the 64-row pipeline with M = 64 UMMAs (64-row blocks only, no split-K)
+  for (int nt : {256, 512})
+    for (int sched = 0; sched < 2; ++sched) add(3, nt, 0, 0, sched, 1);
   return t;
 }
 
@@ -68,6 +72,7 @@ spmm_status spmm_config_supported(int bR, spmm_dtype dtype, int N, const spmm_co
   bool ok = false;
   if (cfg->kernel == 1) ok = cfg->split_k <= 1 && mma_supported(bR, dtype, N, *cfg);
   else if (cfg->kernel == 2) ok = tc_supported(bR, dtype, N, *cfg);
+  else if (cfg->kernel == 3) ok = tc64_supported(bR, dtype, N, *cfg);
   return ok ? SPMM_OK : SPMM_ERR_UNSUPPORTED;
 }
 

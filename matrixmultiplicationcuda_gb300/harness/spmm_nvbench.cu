@@ -140,6 +140,8 @@ std::string config_name(const spmm_config* c) {
   char b[128];
   if (c->kernel == 1)
     std::snprintf(b, sizeof(b), "mma nt%d st%d", c->n_tile, c->stages);
+  else if (c->kernel == 3)
+    std::snprintf(b, sizeof(b), "tc64 nt%d %s", c->n_tile, c->schedule ? "queue" : "static");
   else
     std::snprintf(b, sizeof(b), "tc nt%d st%d acc%d %s split%d", c->n_tile, c->stages, c->acc_buffers,
                   c->schedule ? "queue" : "static", c->split_k > 1 ? c->split_k : 1);

@@ -1,0 +1,128 @@
+"""One representative launch sequence per kernel family, for ncu captures.
+
+    python -m matrixmultiplicationcuda_gb300.profile_kernels [--only NAME,...] [--launches 3]
+
+Families (seeded synthetic inputs; a few hundred MB on the device at most):
+  tc        k_bcsr_tc: A 16384^2, 64x16 blocks, random 2 %, N 512, fp16, the
+            cost model's configuration (512-column tile, one accumulator)
+  tc_split  k_bcsr_tc in split fp16 (three MMAs per block), same product
+  mma_e4m3  k_bcsr_mma: the same product in e4m3 with per-block scales
+  mma16     k_bcsr_mma: A 8192^2, 16x16 blocks, random 5 %, N 1024, fp16
+  batch     k_bcsr_tc_batch: the 64-product uneven workload, one launch
+  convert   k_dense_to_bcsr (count and fill) + k_scan_counts: dense fp16
+            8192 x 8192 (134 MB) with 16x16 blocks at 5 %
+  quantize  k_to_f16 / k_to_bf16 / k_absmax / k_to_e4m3: 64 M fp32 values
+  mlp       the cost model's forward / backward / AdamW kernels, batch 2000
+Each family runs `--launches` times after one warm-up, then synchronises and
+checks the device error word.
+"""
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp")
+    ap.add_argument("--launches", type=int, default=3)
+    args = ap.parse_args(argv)
+    import torch
+    import matrixmultiplicationcuda_gb300 as m
+    from matrixmultiplicationcuda_gb300 import costmodel
+    dev = torch.device("cuda", 0)
+    only = set(args.only.split(","))
+    L = args.launches
+
+    def c3(dtype):
+        M = K = 16384
+        N = 512
+        rp, ci = m.gen_structure(M, K, 64, m.PATTERN_RANDOM, 0.02, 0, seed=20240)
+        vals = m.gen_values(len(ci), 64, 16, m.DIST_SCALED_NORMAL, seed=20241)
+        Bf = m.gen_dense(K, N, m.DIST_NORMAL, seed=20242)
+        A = m.BCSR.from_host(M, K, 64, rp, ci, vals, dtype, device=dev)
+        Bq, Blo, Bs = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), dtype)
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        return A, Bq.view(K, N), (Blo.view(K, N) if Blo is not None else None), \
+            (float(Bs[0]) if Bs is not None else 1.0), C
+
+    def run(fn):
+        fn()
+        torch.cuda.synchronize()
+        for _ in range(L):
+            fn()
+        torch.cuda.synchronize()
+        m.device_error_check()
+
+    if "tc" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16)
+        cfg = m.Config(kernel=2, n_tile=512, acc_buffers=1)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=cfg))
+        print("tc: nnzb=%d" % A.nnzb)
+    if "tc_split" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16_SPLIT)
+        cfg = m.Config(kernel=2, n_tile=256, acc_buffers=2, stages=2)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=cfg, B_lo=Blo))
+        print("tc_split: nnzb=%d" % A.nnzb)
+    if "mma_e4m3" in only:
+        A, B, Blo, bs, C = c3(m.DType.E4M3)
+        cfg = m.Config(kernel=1, n_tile=128, stages=4)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=cfg, b_scale=bs))
+        print("mma_e4m3: nnzb=%d" % A.nnzb)
+    if "mma16" in only:
+        M = K = 8192
+        N = 1024
+        rp, ci = m.gen_structure(M, K, 16, m.PATTERN_RANDOM, 0.05, 0, seed=7)
+        vals = m.gen_values(len(ci), 16, 16, m.DIST_UNIFORM, seed=8)
+        A = m.BCSR.from_host(M, K, 16, rp, ci, vals, m.DType.F16, device=dev)
+        B = torch.from_numpy(m.gen_dense(K, N, m.DIST_UNIFORM, seed=9)).to(dev).half()
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        cfg = m.Config(kernel=1, n_tile=256, stages=4)
+        run(lambda: m.spmm(A, B, N=N, C=C, cfg=cfg))
+        print("mma16: nnzb=%d" % A.nnzb)
+    if "batch" in only:
+        probs = []
+        for sp in m.uneven_batch_specs(64, seed=2024):
+            rp, ci, vals, Bf = m.make_problem(sp)
+            A = m.BCSR.from_host(sp["M"], sp["K"], sp["bR"], rp, ci, vals, m.DType.F16, device=dev)
+            probs.append((A, torch.from_numpy(Bf).to(dev).half(),
+                          torch.empty((sp["M"], sp["N"]), dtype=torch.float32, device=dev)))
+        plan = m.BatchPlan(probs)
+        run(plan.run)
+        plan.close()
+        print("batch: %d problems" % len(probs))
+    if "convert" in only:
+        M = K = 8192
+        rp, ci = m.gen_structure(M, K, 16, m.PATTERN_RANDOM, 0.05, 0, seed=11)
+        vals = m.gen_values(len(ci), 16, 16, m.DIST_UNIFORM, seed=12)
+        dense = torch.zeros((M, K), dtype=torch.float16, device=dev)
+        blocks = torch.from_numpy(vals.reshape(-1, 16, 16)).to(dev).half()
+        rows = np.repeat(np.arange(M // 16), np.diff(rp))
+        view = dense.view(M // 16, 16, K // 16, 16).permute(0, 2, 1, 3)
+        view[torch.from_numpy(rows).to(dev), torch.from_numpy(ci.astype(np.int64)).to(dev)] = blocks
+        run(lambda: m.dense_to_bcsr(dense, 16, 16))
+        print("convert: %d x %d, nnzb=%d" % (M, K, len(ci)))
+    if "quantize" in only:
+        src = torch.randn(64 << 20, device=dev) * 10
+        for dt in (m.DType.F16, m.DType.BF16, m.DType.E4M3):
+            run(lambda: m.quantize(src, dt, block_elems=1024))
+        print("quantize: %d values" % src.numel())
+    if "mlp" in only:
+        s = costmodel.shape()
+        rng = np.random.default_rng(0)
+        p = costmodel.init_params(s, np.zeros(s.in_, np.float32), np.ones(s.in_, np.float32))
+        net = costmodel.MLP(s, p, device=dev)
+        X = torch.from_numpy(rng.standard_normal((2000, s.in_)).astype(np.float32)).to(dev)
+        T = torch.from_numpy(rng.standard_normal((2000, s.out)).astype(np.float32)).to(dev)
+        Mk = torch.ones_like(T)
+        run(lambda: net.forward(X))
+        run(lambda: net.loss_grad(X, T, Mk))
+        print("mlp: batch 2000")
+
+
+if __name__ == "__main__":
+    main()

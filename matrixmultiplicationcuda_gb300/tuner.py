@@ -40,6 +40,8 @@ def config_key(c):
 def config_name(c):
     if c.kernel == 1:
         return "mma nt%d st%d" % (c.n_tile, c.stages)
+    if c.kernel == 3:
+        return "tc64 nt%d %s" % (c.n_tile, "queue" if c.schedule else "static")
     return "tc nt%d st%s acc%d %s split%d" % (c.n_tile, c.stages or "d", c.acc_buffers,
                                              "queue" if c.schedule else "static", max(c.split_k, 1))
 

@@ -80,7 +80,7 @@ def test_features_reject_bad_structure():
 
 def test_config_table():
     cs = tuner.configs()
-    assert len(cs) == 37
+    assert len(cs) == 41
     keys = {tuner.config_key(c) for c in cs}
     assert len(keys) == len(cs)
     for bR in (16, 32, 64):
@@ -88,7 +88,7 @@ def test_config_table():
             mask = tuner.supported_mask(bR, dt, 512)
             assert mask.any()
             assert mask[tuner.default_index(bR, dt, 512)]
-    assert tuner.supported_mask(64, m.DType.F16, 512).sum() == 36
+    assert tuner.supported_mask(64, m.DType.F16, 512).sum() == 40
 
 
 def test_tune_db_roundtrip(tmp_path):

@@ -65,3 +65,31 @@ def test_quantize_e4m3_scales(dev):
     torch.cuda.synchronize()
     assert sc.cpu().tolist() == [1.0, 3.0]
     assert q.cpu().numpy()[31] == 0xFE  # -448 in e4m3
+
+
+@pytest.mark.parametrize("count,offset", [(4096, 0), (4099, 0), (1003, 1), (257, 3), (3, 0)])
+def test_quantize_matches_torch_rounding(dev, count, offset):
+    """The conversions are round-to-nearest-even, element by element, whether
+    they take the 16-byte path (aligned, four at a time) or the scalar one
+    (misaligned source or the last count % 4 values)."""
+    base = (torch.randn(count + offset + 8, device=dev) * 37.0)
+    x = base[offset:offset + count]
+    h, lo, _ = m.quantize(x, m.DType.F16_SPLIT)
+    ref_h = x.half()
+    assert torch.equal(h.view(torch.int16), ref_h.view(torch.int16))
+    assert torch.equal(lo.view(torch.int16), (x - ref_h.float()).half().view(torch.int16))
+    b, _, _ = m.quantize(x, m.DType.BF16)
+    assert torch.equal(b.view(torch.int16), x.bfloat16().view(torch.int16))
+    q, _, sc = m.quantize(x, m.DType.E4M3, block_elems=64)
+    scales = sc.repeat_interleave(64)[:count]
+    ref_q = (x / scales).to(torch.float8_e4m3fn).view(torch.uint8)
+    assert torch.equal(q, ref_q)
+
+
+def test_quantize_single_large_scale_block(dev):
+    """One scale over many elements (how B is scaled for e4m3): the chunked
+    reduction finds the exact maximum."""
+    x = torch.randn(3_000_001, device=dev)
+    x[1_234_567] = -99.5
+    _, _, sc = m.quantize(x, m.DType.E4M3, block_elems=x.numel())
+    assert sc.numel() == 1 and float(sc[0]) == pytest.approx(99.5 / 448.0, rel=1e-7)

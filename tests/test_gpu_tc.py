@@ -107,3 +107,37 @@ def test_tc_split_k(dev, bR, nt, name, acc, split, queue):
     assert mx <= 3e-5 and fr <= 3e-5, (mx, fr)
     for br in np.nonzero(np.diff(rp) == 0)[0][:4]:
         assert np.all(got[br * bR:(br + 1) * bR] == 0)
+
+
+TC64_CASES = [(256, "f16", 5), (256, "f16", 8), (512, "f16", 5), (512, "f16", 4), (256, "bf16", 5),
+              (512, "bf16", 4), (256, "split", 5), (512, "split", 2)]
+
+
+@pytest.mark.parametrize("nt,name,stages", TC64_CASES)
+@pytest.mark.parametrize("N,K,dens,queue,split", [(64, 1024, 0.06, 1, 1), (200, 1024, 0.06, 0, 1),
+                                                  (512, 1024, 0.06, 0, 1), (512, 4096, 0.2, 1, 1),
+                                                  (512, 8192, 0.2, 1, 1)])
+def test_tc64_matches_fp64(dev, nt, name, stages, N, K, dens, queue, split):
+    """The 64-row pipeline with M = 64 UMMAs (kernel 3): partial column tiles,
+    N not a multiple of 64 (2-D panel copies), rows of ~400 blocks, the work
+    queue."""
+    M, bR = 512, 64
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, dens, 1.5, seed=N + K + nt)
+    vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=3)
+    Bf = m.gen_dense(K, N, m.DIST_UNIFORM, seed=4)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, DT[name], device=dev)
+    Bq, Blo, _ = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), DT[name])
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    m.spmm(A, Bq.view(K, N), N=N, C=C, B_lo=Blo.view(K, N) if Blo is not None else None,
+           cfg=m.Config(kernel=3, n_tile=nt, stages=stages, schedule=queue, split_k=split))
+    m.device_error_check()
+    got = C.cpu().numpy()
+    ref = oracle.bcsr_matmul_f64(rp, ci, rounded(vals, name), bR, 16, rounded(Bf, name))
+    assert np.isfinite(got).all()
+    mx, fr = oracle.rel_errors(got, ref)
+    # split: fp32 accumulation over ~1000 products per output (sqrt(1000) x 2^-24
+    # ~ 2e-6); the M = 64 instructions sum in another order than M = 128
+    bar = (5e-6 if name == "split" else 1e-5) if K <= 1024 else 3e-5
+    assert mx <= bar and fr <= bar, (mx, fr)
+    for br in np.nonzero(np.diff(rp) == 0)[0][:4]:
+        assert np.all(got[br * bR:(br + 1) * bR] == 0)
