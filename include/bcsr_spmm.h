@@ -183,6 +183,24 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count,
 spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream);
 spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
 
+/* ---- hybrid BCSR + CSR (HCSRMatrix, formats/HCSRMatrix.cpp:10-36) -------------
+ * C = A_blocks B + A_rest B in ONE launch: the tcgen05 pipeline multiplies the
+ * BCSR part (any block height; the reference uses 16 x 16) and its epilogue
+ * adds the CSR part's entries of each row before C is stored. The reference
+ * runs three kernels (CSR into a second buffer, BCSR into C, then an
+ * element-wise add; main.cu:567-590). fp16 only, no split-K. Both parts
+ * describe the same M x K matrix; A_rest->row_ptr has M + 1 entries, col_idx
+ * holds column indices (not the reference's i % rows). */
+typedef struct spmm_csr_desc {
+  int M, K;
+  const int* row_ptr;
+  const int* col_idx;
+  const void* vals;      /* fp16 */
+} spmm_csr_desc;
+spmm_status spmm_hcsr_mm(const spmm_bcsr_desc* A_blocks, const spmm_csr_desc* A_rest,
+                         const spmm_dense_desc* B, int N, float* C, int ldc,
+                         const spmm_config* cfg, void* stream);
+
 /* ---- tuning ----------------------------------------------------------------------
  * No counterpart in the reference (its harness sweeps kernels by hand).
  * The configuration space: a fixed table of spmm_tune_config_count() entries

@@ -66,6 +66,20 @@ class BCSRMatrix {
   void copyToDevice(int** gpuHdr, int** gpuIdx, half** gpuData) const;
 };
 
+// HCSRMatrix(matrix, threshold) (formats/HCSRMatrix.cpp:10-36): the 16x16
+// blocks whose density (nonzero elements / 256) is >= threshold form a 16x16
+// BCSR part, every other element a CSR part. spmm_hcsr_mm multiplies both
+// parts in one launch.
+class HCSRMatrix {
+ public:
+  BCSRMatrix* bcsr = nullptr;
+  CSRMatrix* csr = nullptr;
+  HCSRMatrix(const Matrix& matrix, float threshold);
+  ~HCSRMatrix();
+  HCSRMatrix(const HCSRMatrix&) = delete;
+  HCSRMatrix& operator=(const HCSRMatrix&) = delete;
+};
+
 // blockDensity (miscutil.cpp:76-87): fraction of elements of the bR x bC block
 // at (i, j) whose value compares != 0.
 float blockDensity(const Matrix& matrix, int i, int j, int blockSizeRow = 16, int blockSizeCol = 16);

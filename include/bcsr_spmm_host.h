@@ -55,6 +55,15 @@ long long spmm_host_dense_to_bcsr(const void* A_half, int rows, int cols, int bR
 long long spmm_host_dense_to_csr(const void* A_half, int rows, int cols, int* hdr, int* idx,
                                  void* vals);
 
+/* HCSRMatrix(matrix, threshold) on the host (formats/HCSRMatrix.cpp:10-36):
+ * 16x16 blocks with density >= threshold form a BCSR part (bhdr[rows/16 + 1],
+ * bidx[nnzb], bvals[nnzb * 256] fp16 bits), all other elements a CSR part
+ * (chdr[rows + 1], cidx[nnz], cvals[nnz]). Call once with NULL arrays for the
+ * sizes. rows and cols must be multiples of 16. Returns 0, or -1. */
+int spmm_host_dense_to_hcsr(const void* A_half, int rows, int cols, float threshold, long long* nnzb,
+                            long long* nnz, int* bhdr, int* bidx, void* bvals, int* chdr, int* cidx,
+                            void* cvals);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,7 @@ from .bcsr import (  # noqa: F401
     device_error_check,
     debug_wait_timeout,
     BatchPlan,
+    hcsr_mm,
 )
 from .host import (  # noqa: F401
     generate_matrix,
@@ -45,6 +46,7 @@ from .host import (  # noqa: F401
     gen_dense,
     host_dense_to_bcsr,
     host_dense_to_csr,
+    host_dense_to_hcsr,
     mat_load,
     mat_save,
     PATTERN_RANDOM,

@@ -44,6 +44,10 @@ class DenseDesc(ctypes.Structure):
     _fields_ = [("data", c_vp), ("data_lo", c_vp), ("scale", c_float), ("ldb", c_int)]
 
 
+class CsrDesc(ctypes.Structure):
+    _fields_ = [("M", c_int), ("K", c_int), ("row_ptr", c_vp), ("col_idx", c_vp), ("vals", c_vp)]
+
+
 class Problem(ctypes.Structure):
     _fields_ = [("A", BcsrDesc), ("B", DenseDesc), ("N", c_int), ("C", c_vp), ("ldc", c_int)]
 
@@ -67,6 +71,8 @@ _SIGS = {
     "spmm_bcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp,
                              c_int, ctypes.POINTER(Config), c_vp]),
     "spmm_bcsr_validate": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_ll, c_vp]),
+    "spmm_hcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(CsrDesc), ctypes.POINTER(DenseDesc), c_int,
+                             c_vp, c_int, ctypes.POINTER(Config), c_vp]),
     "sparseMatrixMulTensor_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor32x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor64x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
@@ -113,6 +119,8 @@ _SIGS = {
     "spmm_mat_save": (c_int, [c_char_p, c_vp, c_int, c_int]),
     "spmm_host_dense_to_bcsr": (c_ll, [c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp]),
     "spmm_host_dense_to_csr": (c_ll, [c_vp, c_int, c_int, c_vp, c_vp, c_vp]),
+    "spmm_host_dense_to_hcsr": (c_int, [c_vp, c_int, c_int, c_float, ctypes.POINTER(c_ll), ctypes.POINTER(c_ll),
+                                        c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
 }
 
 _lib = None

@@ -99,6 +99,29 @@ def spmm(A: BCSR, B, N=None, C=None, cfg: Optional[Config] = None, stream=None, 
     return C
 
 
+def hcsr_mm(A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, B, N=None, C=None,
+            cfg: Optional[Config] = None, stream=None, ldc=None):
+    """Hybrid product C = A_blocks @ B + A_rest @ B in one launch (fp16): the
+    BCSR part on the tensor cores, the CSR part (row_ptr [M+1], col_idx, fp16
+    vals, device tensors) added in the same kernel's epilogue."""
+    from ._lib import CsrDesc
+    torch = _torch()
+    N = int(B.shape[1]) if N is None else int(N)
+    if C is None:
+        C = torch.empty((A_blocks.M, N), dtype=torch.float32, device=B.device)
+    ldc = int(C.stride(0)) if ldc is None else int(ldc)
+    a = A_blocks.desc()
+    r = CsrDesc()
+    r.M, r.K = A_blocks.M, A_blocks.K
+    r.row_ptr = csr_row_ptr.data_ptr()
+    r.col_idx = csr_col_idx.data_ptr() if csr_col_idx.numel() else None
+    r.vals = csr_vals.data_ptr() if csr_vals.numel() else None
+    b = _dense_desc(B, None, 1.0, ldb=B.stride(0))
+    check(lib().spmm_hcsr_mm(ctypes.byref(a), ctypes.byref(r), ctypes.byref(b), N, ctypes.c_void_p(C.data_ptr()),
+                             ldc, ctypes.byref(cfg) if cfg is not None else None, stream_handle(stream)))
+    return C
+
+
 def _ref_launch(fn, hdr, idx, data, B, C, M, N, K, stream, extra=()):
     st = fn(_ptr(hdr), _ptr(idx), _ptr(data), _ptr(B), _ptr(C), int(M), int(N), *extra, int(K),
             stream_handle(stream))

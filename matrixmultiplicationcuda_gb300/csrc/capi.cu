@@ -337,6 +337,47 @@ spmm_status spmm_bcsr_mm(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int 
   return launch_mma(r);
 }
 
+spmm_status spmm_hcsr_mm(const spmm_bcsr_desc* A, const spmm_csr_desc* R, const spmm_dense_desc* B, int N,
+                         float* C, int ldc, const spmm_config* cfg, void* stream) {
+  g_last_error.clear();
+  if (!A || !R || !B) return fail(SPMM_ERR_INVALID_ARG, "null descriptor");
+  if (A->dtype != SPMM_F16) return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product is fp16");
+  if (R->M != A->M || R->K != A->K) return fail(SPMM_ERR_INVALID_ARG, "the two parts must have the same shape");
+  if (A->M > 0 && !R->row_ptr) return fail(SPMM_ERR_INVALID_ARG, "null CSR row_ptr");
+  spmm_config c;
+  std::memset(&c, 0, sizeof(c));
+  if (cfg) c = *cfg;
+  if (c.kernel != 0 && c.kernel != 2) return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product runs on kernel 2");
+  if (c.split_k > 1) return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product has no split-K");
+  c.kernel = 2;
+  // the same argument checks as the BCSR product, then the launch with the CSR part
+  if (A->M < 0 || A->K < 0 || N < 0) return fail(SPMM_ERR_INVALID_ARG, "negative size");
+  if (A->bC != 16 || (A->bR != 16 && A->bR != 32 && A->bR != 64))
+    return fail(SPMM_ERR_UNSUPPORTED, "block shape must be 16, 32 or 64 x 16");
+  if (A->M % A->bR || A->K % 16) return fail(SPMM_ERR_INVALID_ARG, "M / K not multiples of the block shape");
+  if (A->M == 0 || N == 0) return SPMM_OK;
+  if (!A->row_ptr || !C || !B->data) return fail(SPMM_ERR_INVALID_ARG, "null pointer");
+  if (N % 8) return fail(SPMM_ERR_UNSUPPORTED, "N must be a multiple of 8");
+  if (B->ldb < N || B->ldb % 8) return fail(SPMM_ERR_MISALIGNED, "ldb must be >= N and a multiple of 8");
+  if (ldc < N || ldc % 4) return fail(SPMM_ERR_MISALIGNED, "ldc must be >= N and a multiple of 4");
+  if (!aligned(A->vals, 16) || !aligned(B->data, 16) || !aligned(C, 16))
+    return fail(SPMM_ERR_MISALIGNED, "A values, B and C must be 16-byte aligned");
+  if (A->K == 0) {
+    SPMM_CUDA_TRY(cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, A->M, static_cast<cudaStream_t>(stream)));
+    return SPMM_OK;
+  }
+  LaunchRequest r;
+  r.A = A;
+  r.B = B;
+  r.N = N;
+  r.C = C;
+  r.ldc = ldc;
+  r.cfg = c;
+  r.stream = static_cast<cudaStream_t>(stream);
+  r.csr = R;
+  return launch_tc(r);
+}
+
 static spmm_status ref_launch(int bR, const int* hdr, const int* idx, const void* data,
                               const void* B, float* C, unsigned M, unsigned N, unsigned K,
                               void* stream) {

@@ -216,6 +216,28 @@ void BCSRMatrix::copyToDevice(int** gpuHdr, int** gpuIdx, half** gpuData) const 
 }
 
 // ---------------------------------------------------------------------------------
+// Splits the blocks by density into two zero-initialised copies of the matrix,
+// as the reference does, then builds the two formats from them.
+HCSRMatrix::HCSRMatrix(const Matrix& m, float threshold) {
+  if (m.rows % 16 || m.cols % 16)
+    throw std::invalid_argument("HCSRMatrix needs rows and columns that are multiples of 16");
+  Matrix dense_part(m.rows, m.cols), sparse_part(m.rows, m.cols);
+  for (int i = 0; i < m.rows; i += 16)
+    for (int j = 0; j < m.cols; j += 16) {
+      Matrix& dst = blockDensity(m, i, j, 16, 16) >= threshold ? dense_part : sparse_part;
+      for (int x = i; x < i + 16; ++x)
+        std::memcpy(dst.data + (size_t)x * m.cols + j, m.data + (size_t)x * m.cols + j, 16 * sizeof(half));
+    }
+  bcsr = new BCSRMatrix(dense_part, 16, 16);
+  csr = new CSRMatrix(sparse_part);
+}
+
+HCSRMatrix::~HCSRMatrix() {
+  delete bcsr;
+  delete csr;
+}
+
+// ---------------------------------------------------------------------------------
 // C ABI over the classes (used by the Python layer and by callers without C++).
 extern "C" {
 
@@ -269,6 +291,30 @@ long long spmm_host_dense_to_bcsr(const void* A_half, int rows, int cols, int bR
     if (idx) std::memcpy(idx, b.idx, sizeof(int) * nnzb);
     if (vals) std::memcpy(vals, b.data, sizeof(half) * nnzb * bR * bC);
     return nnzb;
+  } catch (const std::exception& e) {
+    spmm::host_fail(SPMM_ERR_INVALID_ARG, e.what());
+    return -1;
+  }
+}
+
+// HCSRMatrix on the host: the sizes of both parts, and their arrays where the
+// output pointers are non-null. Returns 0, or -1 on bad arguments.
+int spmm_host_dense_to_hcsr(const void* A_half, int rows, int cols, float threshold, long long* nnzb,
+                            long long* nnz, int* bhdr, int* bidx, void* bvals, int* chdr, int* cidx, void* cvals) {
+  try {
+    if (!A_half || !nnzb || !nnz || rows < 0 || cols < 0) throw std::invalid_argument("bad arguments");
+    Matrix m(rows, cols);
+    std::memcpy(m.data, A_half, (size_t)rows * cols * sizeof(half));
+    HCSRMatrix h(m, threshold);
+    *nnzb = h.bcsr->hdr[h.bcsr->blockRows];
+    *nnz = h.csr->hdr[rows];
+    if (bhdr) std::memcpy(bhdr, h.bcsr->hdr, sizeof(int) * (h.bcsr->blockRows + 1));
+    if (bidx) std::memcpy(bidx, h.bcsr->idx, sizeof(int) * *nnzb);
+    if (bvals) std::memcpy(bvals, h.bcsr->data, sizeof(half) * *nnzb * 256);
+    if (chdr) std::memcpy(chdr, h.csr->hdr, sizeof(int) * (rows + 1));
+    if (cidx) std::memcpy(cidx, h.csr->idx, sizeof(int) * *nnz);
+    if (cvals) std::memcpy(cvals, h.csr->data, sizeof(half) * *nnz);
+    return 0;
   } catch (const std::exception& e) {
     spmm::host_fail(SPMM_ERR_INVALID_ARG, e.what());
     return -1;

@@ -74,6 +74,8 @@ struct LaunchRequest {
   // allocation-free one): the device error word and the work-queue pair.
   unsigned* err_word = nullptr;
   unsigned* queue = nullptr;
+  // hybrid product: the CSR part added by the tcgen05 pipeline's epilogue
+  const spmm_csr_desc* csr = nullptr;
 };
 // mma.sync family (spmm_mma.cu)
 spmm_status launch_mma(const LaunchRequest& r);

@@ -54,6 +54,13 @@ struct TcParams {
   int panel3d;      // B panel loaded by one 3-D copy (N % 64 == 0)
   unsigned* queue;  // [0] next item, [1] CTAs done; NULL = static item striding
   int split;        // items per (block row, column tile); > 1: partial sums added into C
+  // hybrid (BCSR + CSR): the CSR part's entries are added in the epilogue
+  // (NULL csr_row_ptr = plain BCSR)
+  const int* csr_row_ptr;
+  const int* csr_col_idx;
+  const __half* csr_vals;
+  const __half* Bh;
+  long long ldb;
 };
 
 // BR: block height (the UMMA N); NT: output columns per item; STAGES: ring
@@ -401,6 +408,19 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 #pragma unroll
             for (int i = 0; i < 16; ++i) v[i] = 0.f;
           }
+          if (p.csr_row_ptr && n < p.N) {
+            // the CSR part of these 16 rows: every entry (r, k, a) adds
+            // a * B[k][n] (one B row per entry, read across the lanes)
+#pragma unroll 1
+            for (int i = 0; i < 16; ++i) {
+              const long long r = row0 + c0 + i;
+              const int e1 = __ldg(p.csr_row_ptr + r + 1);
+              for (int e = __ldg(p.csr_row_ptr + r); e < e1; ++e) {
+                const float a = __half2float(p.csr_vals[e]);
+                v[i] = fmaf(a, __half2float(p.Bh[(long long)__ldg(p.csr_col_idx + e) * p.ldb + n]), v[i]);
+              }
+            }
+          }
           if (n < p.N) {
             if (p.split == 1) {
 #pragma unroll
@@ -557,6 +577,13 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.panel3d = panel3d;
   // items: static stride by default, or a work queue on request
   p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
+  p.csr_row_ptr = r.csr ? r.csr->row_ptr : nullptr;
+  p.csr_col_idx = r.csr ? r.csr->col_idx : nullptr;
+  p.csr_vals = r.csr ? static_cast<const __half*>(r.csr->vals) : nullptr;
+  p.Bh = static_cast<const __half*>(B.data);
+  p.ldb = B.ldb;
+  if (r.csr && (p.split > 1 || mode != MODE_F16))
+    return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product runs in fp16 without split-K");
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
   if (p.split > 1)

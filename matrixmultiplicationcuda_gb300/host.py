@@ -61,6 +61,27 @@ def host_dense_to_bcsr(A_half_bits, bR=16, bC=16):
     return hdr, idx[:n], data[:n * bR * bC]
 
 
+def host_dense_to_hcsr(A_half_bits, threshold):
+    """HCSRMatrix(matrix, threshold) (formats/HCSRMatrix.cpp:10-36) on the host:
+    ((hdr, idx, data bits) of the 16x16 BCSR part, (row_ptr, col_idx, vals bits)
+    of the CSR part)."""
+    A = np.ascontiguousarray(A_half_bits).view(np.uint16)
+    rows, cols = A.shape
+    nnzb, nnz = ctypes.c_longlong(0), ctypes.c_longlong(0)
+    if lib().spmm_host_dense_to_hcsr(_vp(A), rows, cols, float(threshold), ctypes.byref(nnzb), ctypes.byref(nnz),
+                                     None, None, None, None, None, None) != 0:
+        raise SpmmError(Status.INVALID_ARG, last_error())
+    bh = np.empty(rows // 16 + 1, np.int32)
+    bi = np.empty(max(nnzb.value, 1), np.int32)
+    bd = np.empty(max(nnzb.value * 256, 1), np.uint16)
+    ch = np.empty(rows + 1, np.int32)
+    cx = np.empty(max(nnz.value, 1), np.int32)
+    cd = np.empty(max(nnz.value, 1), np.uint16)
+    lib().spmm_host_dense_to_hcsr(_vp(A), rows, cols, float(threshold), ctypes.byref(nnzb), ctypes.byref(nnz),
+                                  _vp(bh), _vp(bi), _vp(bd), _vp(ch), _vp(cx), _vp(cd))
+    return (bh, bi[:nnzb.value], bd[:nnzb.value * 256]), (ch, cx[:nnz.value], cd[:nnz.value])
+
+
 def host_dense_to_csr(A_half_bits):
     A = np.ascontiguousarray(A_half_bits).view(np.uint16)
     rows, cols = A.shape

@@ -99,6 +99,28 @@ def bcsr(A_half_bits, bR=16, bC=16):
     return hdr, idx[:n], data[:n * bR * bC]
 
 
+def hcsr(A_half_bits, threshold):
+    """HCSRMatrix(matrix, threshold) restated (formats/HCSRMatrix.cpp:10-36):
+    16x16 blocks whose density -- nonzero elements / 256 as a float, the
+    reference's blockDensity (miscutil.cpp:76-87) -- is >= threshold go to a
+    16x16 BCSR part, every other element to a CSR part (formats/CSRMatrix.cu:
+    13-37, with the column index of element i taken as i % cols). Returns
+    ((hdr, idx, data bits), (row_ptr, col_idx, vals bits))."""
+    A = np.ascontiguousarray(A_half_bits, np.uint16)
+    rows, cols = A.shape
+    nz = (A & 0x7FFF) != 0
+    cnt = nz.reshape(rows // 16, 16, cols // 16, 16).sum(axis=(1, 3))
+    dense_blk = (cnt.astype(np.float32) / np.float32(256.0)) >= np.float32(threshold)
+    mask = np.repeat(np.repeat(dense_blk, 16, axis=0), 16, axis=1)
+    A1 = np.where(mask, A, np.uint16(0)).astype(np.uint16)
+    A2 = np.where(mask, np.uint16(0), A).astype(np.uint16)
+    part_b = bcsr(A1, 16, 16)
+    nz2 = (A2 & 0x7FFF) != 0
+    rp = np.concatenate([[0], np.cumsum(nz2.sum(axis=1))]).astype(np.int32)
+    r, c = np.nonzero(nz2)
+    return part_b, (rp, c.astype(np.int32), A2[r, c].astype(np.uint16))
+
+
 def cpu_matmul_ref(A_bits, B_bits, row0=0, row1=None, threads=1):
     """cpu_matmul_ref (nvbench_main.cu:78-91) for rows [row0, row1)."""
     A = np.ascontiguousarray(A_bits, np.uint16)

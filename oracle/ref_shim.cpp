@@ -11,6 +11,7 @@
 #include "Matrix.cuh"
 #include "formats/BCSRMatrix.cuh"
 #include "formats/CSRMatrix.cuh"
+#include "formats/HCSRMatrix.h"
 #include "miscutil.h"
 #include "matrix_generator.h"
 
@@ -52,6 +53,26 @@ long long ref_bcsr(const uint16_t* A, int rows, int cols, int bR, int bC,
   } catch (...) {
     return -1;
   }
+}
+
+// HCSRMatrix(matrix, threshold): sizes of both parts, and their arrays when the
+// output pointers are non-null (the CSR part's idx as the reference stores it).
+int ref_hcsr(const uint16_t* A, int rows, int cols, float threshold, long long* nnzb, long long* nnz,
+             int* bhdr, int* bidx, uint16_t* bdata, int* chdr, int* cidx, uint16_t* cdata) {
+  Matrix m(rows, cols);
+  std::memcpy(m.data, A, sizeof(uint16_t) * (size_t)rows * cols);
+  HCSRMatrix h(m, threshold);
+  *nnzb = h.bcsr->hdr[h.bcsr->blockRows];
+  *nnz = h.csr->hdr[rows];
+  if (bhdr) std::memcpy(bhdr, h.bcsr->hdr, sizeof(int) * (h.bcsr->blockRows + 1));
+  if (bidx) std::memcpy(bidx, h.bcsr->idx, sizeof(int) * *nnzb);
+  if (bdata) std::memcpy(bdata, h.bcsr->data, sizeof(uint16_t) * *nnzb * 256);
+  if (chdr) std::memcpy(chdr, h.csr->hdr, sizeof(int) * (rows + 1));
+  if (cidx) std::memcpy(cidx, h.csr->idx, sizeof(int) * *nnz);
+  if (cdata) std::memcpy(cdata, h.csr->data, sizeof(uint16_t) * *nnz);
+  delete h.bcsr;
+  delete h.csr;
+  return 0;
 }
 
 float ref_block_density(const uint16_t* A, int rows, int cols, int i, int j, int bR, int bC) {

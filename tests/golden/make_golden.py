@@ -14,7 +14,9 @@ What is stored (all produced by the reference's sources, not by the oracle):
   * the 1024 x 1024 blockrandom workload (16x16 blocks, 10% kept, seed 123):
     row_ptr, col_idx and a SHA-256 of the stored fp16 block values;
   * Matrix(".mat path") of a small text file (rows, cols, nonZeros, half bits);
-  * maxdiff / avgrelerr / rmse (miscutil.cpp:35-74) on a 16 x 16 pair.
+  * maxdiff / avgrelerr / rmse (miscutil.cpp:35-74) on a 16 x 16 pair;
+  * HCSRMatrix(matrix, threshold) (formats/HCSRMatrix.cpp:10-36) of a 128 x 128
+    matrix with mixed block densities, at six thresholds: both parts' arrays.
 """
 import ctypes
 import hashlib
@@ -135,6 +137,37 @@ def main(ref_tree):
     out["metrics/a"], out["metrics/b"] = a, b
     out["metrics/values"] = np.array([R.ref_maxdiff(p(a), p(b), 16), R.ref_avgrelerr(p(a), p(b), 16),
                                       R.ref_rmse(p(a), p(b), 16)], np.float64)
+    # HCSRMatrix(matrix, threshold) (formats/HCSRMatrix.cpp:10-36) on square
+    # matrices whose 16x16 blocks have mixed densities: a random-pattern matrix
+    # (element density 0.7) with every third block row thinned to 25 %
+    R.ref_hcsr.restype = ctypes.c_int
+    R.ref_hcsr.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float] + [ctypes.c_void_p] * 8
+    def gen(r, c, sp, pat, bs, seed):
+        m = np.empty((r, c), np.float32)
+        assert R.ref_generate_matrix(r, c, sp, pat.encode(), bs, seed, p(m)) == 0
+        return m
+
+    dense = gen(128, 128, 0.3, "random", 16, 11)
+    thin = gen(128, 128, 0.75, "random", 16, 12)
+    mixed = dense.copy()
+    for br in range(0, 8, 3):
+        mixed[br * 16:(br + 1) * 16] = thin[br * 16:(br + 1) * 16]
+    hb = to_half(mixed)
+    out["hcsr/A"] = hb
+    for th in (0.0, 0.2, 0.5, 0.65, 0.8, 1.1):
+        nnzb, nnz = ctypes.c_longlong(), ctypes.c_longlong()
+        R.ref_hcsr(p(hb), 128, 128, th, ctypes.byref(nnzb), ctypes.byref(nnz), *([None] * 6))
+        bh = np.zeros(9, np.int32)
+        bi = np.zeros(max(nnzb.value, 1), np.int32)
+        bd = np.zeros(max(nnzb.value * 256, 1), np.uint16)
+        ch = np.zeros(129, np.int32)
+        cx = np.zeros(max(nnz.value, 1), np.int32)
+        cd = np.zeros(max(nnz.value, 1), np.uint16)
+        R.ref_hcsr(p(hb), 128, 128, th, ctypes.byref(nnzb), ctypes.byref(nnz), p(bh), p(bi), p(bd), p(ch), p(cx),
+                   p(cd))
+        key = "hcsr/%g" % th
+        out[key + "/bhdr"], out[key + "/bidx"], out[key + "/bdata"] = bh, bi[:nnzb.value], bd[:nnzb.value * 256]
+        out[key + "/chdr"], out[key + "/cidx"], out[key + "/cdata"] = ch, cx[:nnz.value], cd[:nnz.value]
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes,", len(out), "arrays")

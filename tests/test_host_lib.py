@@ -168,7 +168,9 @@ int main() {
   for (int i = 0; i < 128; ++i) for (int j = 0; j < 96; ++j) A.data[i * 96 + j] = __float2half(g[i][j]);
   BCSRMatrix b(A, 32, 16);
   CSRMatrix c(A);
-  std::printf("%d %d %d %d %d\n", b.blockRows, b.blockCols, b.hdr[b.blockRows], b.nonZeros, c.hdr[128]);
+  HCSRMatrix h(A, 0.5f);
+  std::printf("%d %d %d %d %d %d %d\n", b.blockRows, b.blockCols, b.hdr[b.blockRows], b.nonZeros, c.hdr[128],
+              h.bcsr->hdr[h.bcsr->blockRows], h.csr->hdr[128]);
   try { BCSRMatrix bad(A, 8, 16); return 3; } catch (const std::invalid_argument&) {}
   return 0;
 }
@@ -182,11 +184,13 @@ int main() {
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
-    br, bc, nnzb, nz, csr_nnz = map(int, out.stdout.split())
+    br, bc, nnzb, nz, csr_nnz, h_nnzb, h_nnz = map(int, out.stdout.split())
     A = oracle.f32_to_f16(oracle.generate_matrix(128, 96, 0.6, "blockrandom", 16, 123))
     hdr, idx, data = oracle.bcsr(A, 32, 16)
     assert (br, bc, nnzb, nz) == (4, 6, len(idx), len(idx) * 512)
     assert csr_nnz == int(np.count_nonzero(A & 0x7fff))
+    (_, hidx, _), (_, cidx, _) = oracle.hcsr(A.view(np.uint16).reshape(128, 96), 0.5)
+    assert (h_nnzb, h_nnz) == (len(hidx), len(cidx))
 
 
 def test_harness_built_and_prints_usage():
@@ -194,3 +198,27 @@ def test_harness_built_and_prints_usage():
     assert os.path.exists(exe)
     r = subprocess.run([exe, "--help"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "--preset" in r.stderr
+
+
+@pytest.mark.parametrize("th", ["0", "0.2", "0.5", "0.65", "0.8", "1.1"])
+def test_hcsr_matches_reference_golden(golden, th):
+    """HCSRMatrix(matrix, threshold): the oracle restatement and the library's
+    host class give the reference's own arrays for both parts."""
+    A = golden["hcsr/A"]
+    want = [golden["hcsr/%s/%s" % (th, k)] for k in ("bhdr", "bidx", "bdata", "chdr", "cidx", "cdata")]
+    (ob, oc) = oracle.hcsr(A, float(th))
+    (hb, hc) = m.host_dense_to_hcsr(A, float(th))
+    for got in (list(ob) + list(oc), list(hb) + list(hc)):
+        for g, w in zip(got, want):
+            np.testing.assert_array_equal(g, w)
+
+
+def test_hcsr_non_square_and_errors():
+    A = oracle.f32_to_f16(oracle.generate_matrix(96, 160, 0.5, "random", 16, 3)).view(np.uint16).reshape(96, 160)
+    (hb, hc) = m.host_dense_to_hcsr(A, 0.5)
+    (ob, oc) = oracle.hcsr(A, 0.5)
+    for g, w in zip(list(hb) + list(hc), list(ob) + list(oc)):
+        np.testing.assert_array_equal(g, w)
+    assert hc[1].max() < 160          # column indices, not the reference's i % rows
+    with pytest.raises(m.SpmmError):
+        m.host_dense_to_hcsr(np.zeros((40, 64), np.uint16), 0.5)
