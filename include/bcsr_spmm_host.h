@@ -55,6 +55,37 @@ long long spmm_host_dense_to_bcsr(const void* A_half, int rows, int cols, int bR
 long long spmm_host_dense_to_csr(const void* A_half, int rows, int cols, int* hdr, int* idx,
                                  void* vals);
 
+/* Matrix Market files (.mtx): what the reference's generator writes through
+ * scipy's mmwrite (matrix_generator.py:100-108). Coordinate (real, integer or
+ * pattern; general, symmetric or skew-symmetric) and array (real, general)
+ * files; repeated entries are summed.
+ *   read_header: rows, cols, stored entries.
+ *   load:        into a dense row-major fp16 matrix (as Matrix(".mat")).
+ *   load_bcsr:   straight into BCSR (bR x bC blocks, fp16, a block kept when
+ *                a value in it rounds to a nonzero fp16) without a dense copy:
+ *                call with col_idx / vals NULL (or capacity_blocks < nnzb)
+ *                for rows, cols, row_ptr (rows/bR + 1 ints) and nnzb, then
+ *                with room for nnzb blocks.
+ *   save:        a dense fp32 matrix as coordinate real general. */
+spmm_status spmm_mtx_read_header(const char* path, int* rows, int* cols, long long* entries);
+spmm_status spmm_mtx_load(const char* path, void* out_half, size_t capacity, int* rows, int* cols,
+                          int* nonZeros);
+spmm_status spmm_mtx_load_bcsr(const char* path, int bR, int bC, int* rows, int* cols, int* row_ptr,
+                               long long* nnzb, int* col_idx, void* vals, long long capacity_blocks);
+spmm_status spmm_mtx_save(const char* path, const float* vals, int rows, int cols);
+
+/* Binary BCSR file: "SPMMBCS1", int32 M, K, bR, bC, dtype, 0, int64 nnzb,
+ * then row_ptr, col_idx, vals (nnzb*bR*bC elements of the dtype), vals_lo
+ * (F16_SPLIT) and scales (E4M3), little-endian, as they lie in memory. load:
+ * call with NULL arrays (or capacity_blocks < nnzb) for the header, then with
+ * room for nnzb blocks. */
+spmm_status spmm_bcsr_save(const char* path, int M, int K, int bR, int bC, int dtype, long long nnzb,
+                           const int* row_ptr, const int* col_idx, const void* vals, const void* vals_lo,
+                           const float* scales);
+spmm_status spmm_bcsr_load(const char* path, int* M, int* K, int* bR, int* bC, int* dtype,
+                           long long* nnzb, int* row_ptr, int* col_idx, void* vals, void* vals_lo,
+                           float* scales, long long capacity_blocks);
+
 /* HCSRMatrix(matrix, threshold) on the host (formats/HCSRMatrix.cpp:10-36):
  * 16x16 blocks with density >= threshold form a BCSR part (bhdr[rows/16 + 1],
  * bidx[nnzb], bvals[nnzb * 256] fp16 bits), all other elements a CSR part

@@ -47,6 +47,11 @@ from .host import (  # noqa: F401
     host_dense_to_bcsr,
     host_dense_to_csr,
     host_dense_to_hcsr,
+    mtx_load,
+    mtx_load_bcsr,
+    mtx_save,
+    bcsr_save,
+    bcsr_load,
     mat_load,
     mat_save,
     PATTERN_RANDOM,

@@ -119,6 +119,15 @@ _SIGS = {
     "spmm_mat_save": (c_int, [c_char_p, c_vp, c_int, c_int]),
     "spmm_host_dense_to_bcsr": (c_ll, [c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp]),
     "spmm_host_dense_to_csr": (c_ll, [c_vp, c_int, c_int, c_vp, c_vp, c_vp]),
+    "spmm_mtx_read_header": (c_int, [c_char_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_ll)]),
+    "spmm_mtx_load": (c_int, [c_char_p, c_vp, c_size, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                              ctypes.POINTER(c_int)]),
+    "spmm_mtx_load_bcsr": (c_int, [c_char_p, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_vp,
+                                   ctypes.POINTER(c_ll), c_vp, c_vp, c_ll]),
+    "spmm_mtx_save": (c_int, [c_char_p, c_vp, c_int, c_int]),
+    "spmm_bcsr_save": (c_int, [c_char_p, c_int, c_int, c_int, c_int, c_int, c_ll, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "spmm_bcsr_load": (c_int, [c_char_p] + [ctypes.POINTER(c_int)] * 5 + [ctypes.POINTER(c_ll), c_vp, c_vp, c_vp,
+                                                                          c_vp, c_vp, c_ll]),
     "spmm_host_dense_to_hcsr": (c_int, [c_vp, c_int, c_int, c_float, ctypes.POINTER(c_ll), ctypes.POINTER(c_ll),
                                         c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
 }

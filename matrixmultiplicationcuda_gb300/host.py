@@ -107,3 +107,65 @@ def mat_load(path):
 def mat_save(path, vals_f32):
     v = np.ascontiguousarray(vals_f32, np.float32)
     check(lib().spmm_mat_save(str(path).encode(), _vp(v), v.shape[0], v.shape[1]))
+
+
+def mtx_load(path):
+    """A Matrix Market file as a dense fp16 matrix: (half bits [rows, cols], nonZeros)."""
+    r, c, n = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_longlong(0)
+    check(lib().spmm_mtx_read_header(str(path).encode(), ctypes.byref(r), ctypes.byref(c), ctypes.byref(n)))
+    out = np.empty((r.value, c.value), np.uint16)
+    nz = ctypes.c_int(0)
+    check(lib().spmm_mtx_load(str(path).encode(), _vp(out), out.size, ctypes.byref(r), ctypes.byref(c),
+                              ctypes.byref(nz)))
+    return out, nz.value
+
+
+def mtx_load_bcsr(path, bR=16, bC=16):
+    """A Matrix Market file straight into BCSR: (rows, cols, row_ptr, col_idx, fp16 value bits)."""
+    r, c, n = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_longlong(0)
+    check(lib().spmm_mtx_read_header(str(path).encode(), ctypes.byref(r), ctypes.byref(c), ctypes.byref(n)))
+    rp = np.empty(r.value // bR + 1, np.int32)
+    nnzb = ctypes.c_longlong(0)
+    check(lib().spmm_mtx_load_bcsr(str(path).encode(), bR, bC, ctypes.byref(r), ctypes.byref(c), _vp(rp),
+                                   ctypes.byref(nnzb), None, None, 0))
+    ci = np.empty(max(nnzb.value, 1), np.int32)
+    vals = np.empty(max(nnzb.value * bR * bC, 1), np.uint16)
+    check(lib().spmm_mtx_load_bcsr(str(path).encode(), bR, bC, ctypes.byref(r), ctypes.byref(c), _vp(rp),
+                                   ctypes.byref(nnzb), _vp(ci), _vp(vals), nnzb.value))
+    return r.value, c.value, rp, ci[:nnzb.value], vals[:nnzb.value * bR * bC]
+
+
+def mtx_save(path, vals_f32):
+    v = np.ascontiguousarray(vals_f32, np.float32)
+    check(lib().spmm_mtx_save(str(path).encode(), _vp(v), v.shape[0], v.shape[1]))
+
+
+def bcsr_save(path, M, K, bR, bC, row_ptr, col_idx, vals, dtype=0, vals_lo=None, scales=None):
+    """The binary BCSR file (host arrays; vals as raw element bits)."""
+    arrs = [np.ascontiguousarray(a) for a in (row_ptr, col_idx, vals)]
+    lo = np.ascontiguousarray(vals_lo) if vals_lo is not None else None
+    sc = np.ascontiguousarray(scales, np.float32) if scales is not None else None
+    check(lib().spmm_bcsr_save(str(path).encode(), M, K, bR, bC, int(dtype), len(arrs[1]), _vp(arrs[0]),
+                               _vp(arrs[1]) if len(arrs[1]) else None, _vp(arrs[2]) if arrs[2].size else None,
+                               _vp(lo) if lo is not None else None, _vp(sc) if sc is not None else None))
+
+
+def bcsr_load(path):
+    """(M, K, bR, bC, dtype, row_ptr, col_idx, vals bits, vals_lo bits or None, scales or None)."""
+    h = [ctypes.c_int(0) for _ in range(5)]
+    n = ctypes.c_longlong(0)
+    check(lib().spmm_bcsr_load(str(path).encode(), *[ctypes.byref(x) for x in h], ctypes.byref(n),
+                               None, None, None, None, None, 0))
+    M, K, bR, bC, dt = (x.value for x in h)
+    esz = np.uint8 if dt == 2 else np.uint16
+    rp = np.empty(M // bR + 1, np.int32)
+    ci = np.empty(max(n.value, 1), np.int32)
+    vals = np.empty(max(n.value * bR * bC, 1), esz)
+    lo = np.empty(max(n.value * bR * bC, 1), np.uint16) if dt == 3 else None
+    sc = np.empty(max(n.value, 1), np.float32) if dt == 2 else None
+    check(lib().spmm_bcsr_load(str(path).encode(), *[ctypes.byref(x) for x in h], ctypes.byref(n), _vp(rp), _vp(ci),
+                               _vp(vals), _vp(lo) if lo is not None else None, _vp(sc) if sc is not None else None,
+                               n.value))
+    k = n.value
+    return (M, K, bR, bC, dt, rp, ci[:k], vals[:k * bR * bC], lo[:k * bR * bC] if lo is not None else None,
+            sc[:k] if sc is not None else None)
