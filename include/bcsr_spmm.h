@@ -156,6 +156,31 @@ spmm_status spmm_dense_to_bcsr_count(const void* A, int M, int K, int lda, int b
 spmm_status spmm_dense_to_bcsr_fill(const void* A, int M, int K, int lda, int bR, int bC,
                                     const int* row_ptr, int* col_idx, void* vals, void* stream);
 
+/* ---- generators on the GPU ------------------------------------------------------
+ * The host generators' counter-based streams (bcsr_spmm_host.h), evaluated on
+ * the device, for inputs too large to generate on the host quickly.
+ *   gen_structure: as spmm_gen_structure into device row_ptr (M/bR + 1) and
+ *     col_idx (capacity entries; skipped when too small or NULL); *nnzb_out is
+ *     always set (synchronises the stream). Random, band and block-diagonal
+ *     structures are bit-identical to the host's; log-normal row counts go
+ *     through device log / exp, so one may differ by one from the host's.
+ *   gen_values / gen_dense: as spmm_gen_values / spmm_gen_dense (uniform
+ *     values bit-identical, normal ones the same transform).
+ *   generate_matrix: a dense fp16 matrix in one of the reference generator's
+ *     patterns (matrix_generator.cpp:28-140) with the counter-based stream
+ *     instead of mt19937: the same shapes and value distribution, not the
+ *     reference's bits (spmm_generate_matrix is the bit-identical host one). */
+spmm_status spmm_gpu_gen_structure(int M, int K, int bR, int pattern, double density, double param,
+                                   unsigned long long seed, int* row_ptr, int* col_idx,
+                                   long long capacity, long long* nnzb_out, void* stream);
+spmm_status spmm_gpu_gen_values(long long nnzb, int bR, int bC, int dist, unsigned long long seed,
+                                float* out, void* stream);
+spmm_status spmm_gpu_gen_dense(long long count, int dist, unsigned long long seed, float* out,
+                               void* stream);
+spmm_status spmm_gpu_generate_matrix(int rows, int cols, double sparsity, const char* pattern,
+                                     int blocksize, unsigned long long seed, void* out_half,
+                                     void* stream);
+
 /* ---- precision conversion (device, asynchronous) ------------------------------
  * From fp32 block values (the exact values before storage rounding):
  *   to fp16 / bf16 (round to nearest even),

@@ -38,6 +38,10 @@ from .bcsr import (  # noqa: F401
     debug_wait_timeout,
     BatchPlan,
     hcsr_mm,
+    gpu_gen_structure,
+    gpu_gen_values,
+    gpu_gen_dense,
+    gpu_generate_matrix,
 )
 from .host import (  # noqa: F401
     generate_matrix,

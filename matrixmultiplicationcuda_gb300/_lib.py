@@ -71,6 +71,11 @@ _SIGS = {
     "spmm_bcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp,
                              c_int, ctypes.POINTER(Config), c_vp]),
     "spmm_bcsr_validate": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_ll, c_vp]),
+    "spmm_gpu_gen_structure": (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, c_ull, c_vp, c_vp, c_ll,
+                                       ctypes.POINTER(c_ll), c_vp]),
+    "spmm_gpu_gen_values": (c_int, [c_ll, c_int, c_int, c_int, c_ull, c_vp, c_vp]),
+    "spmm_gpu_gen_dense": (c_int, [c_ll, c_int, c_ull, c_vp, c_vp]),
+    "spmm_gpu_generate_matrix": (c_int, [c_int, c_int, c_double, c_char_p, c_int, c_ull, c_vp, c_vp]),
     "spmm_hcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(CsrDesc), ctypes.POINTER(DenseDesc), c_int,
                              c_vp, c_int, ctypes.POINTER(Config), c_vp]),
     "sparseMatrixMulTensor_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),

@@ -177,6 +177,45 @@ def dense_to_bcsr(A_half, bR=16, bC=16, stream=None):
     return rp, ci, vals
 
 
+def gpu_gen_structure(M, K, bR, pattern, density, param=0.0, seed=1, device="cuda", stream=None):
+    """BCSR structure generated on the GPU: (row_ptr, col_idx) device tensors
+    (the host gen_structure's streams; see spmm_gpu_gen_structure)."""
+    torch = _torch()
+    rp = torch.empty(M // bR + 1, dtype=torch.int32, device=device)
+    n = ctypes.c_longlong(0)
+    s = stream_handle(stream)
+    check(lib().spmm_gpu_gen_structure(M, K, bR, pattern, float(density), float(param), seed, _ptr(rp), None, 0,
+                                       ctypes.byref(n), s))
+    ci = torch.empty(max(n.value, 1), dtype=torch.int32, device=device)
+    check(lib().spmm_gpu_gen_structure(M, K, bR, pattern, float(density), float(param), seed, _ptr(rp), _ptr(ci),
+                                       n.value, ctypes.byref(n), s))
+    return rp, ci[:n.value]
+
+
+def gpu_gen_values(nnzb, bR, bC=16, dist=0, seed=2, device="cuda", stream=None):
+    torch = _torch()
+    out = torch.empty(nnzb * bR * bC, dtype=torch.float32, device=device)
+    check(lib().spmm_gpu_gen_values(nnzb, bR, bC, dist, seed, _ptr(out), stream_handle(stream)))
+    return out
+
+
+def gpu_gen_dense(rows, cols, dist=0, seed=3, device="cuda", stream=None):
+    torch = _torch()
+    out = torch.empty((rows, cols), dtype=torch.float32, device=device)
+    check(lib().spmm_gpu_gen_dense(rows * cols, dist, seed, _ptr(out), stream_handle(stream)))
+    return out
+
+
+def gpu_generate_matrix(rows, cols, sparsity=0.7, pattern="random", blocksize=16, seed=123, device="cuda",
+                        stream=None):
+    """A dense fp16 matrix in one of the reference generator's patterns, made on the GPU."""
+    torch = _torch()
+    out = torch.empty((rows, cols), dtype=torch.float16, device=device)
+    check(lib().spmm_gpu_generate_matrix(rows, cols, float(sparsity), pattern.encode(), blocksize, seed, _ptr(out),
+                                         stream_handle(stream)))
+    return out
+
+
 def validate(A: BCSR, stream=None):
     check(lib().spmm_bcsr_validate(_ptr(A.row_ptr), _ptr(A.col_idx) if A.nnzb else None, A.M, A.K,
                                    A.bR, A.nnzb, stream_handle(stream)))

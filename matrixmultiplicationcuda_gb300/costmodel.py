@@ -208,12 +208,14 @@ def sample_specs(n, seed):
     return specs
 
 
-def collect(specs, warmup=2, reps=5, device="cuda", progress=None):
+def collect(specs, warmup=2, reps=5, device="cuda", progress=None, gpu_structures=False):
     """Features [n x 18], sweep times [n x configs] (ms, +inf unsupported) and
     stored-block counts of the products in `specs`. Values come from fixed
     random pools (timing does not depend on them; e4m3 operands are the same
     bytes reinterpreted, split products reuse them as the low halves); the
-    structure is generated per product."""
+    structure is generated per product, on the host (the default: the
+    committed dataset regenerates bit for bit there) or with gpu_structures on
+    the GPU (same streams; log-normal row counts may differ by one)."""
     import torch
     from .bcsr import BCSR
     from ._lib import DType
@@ -231,11 +233,17 @@ def collect(specs, warmup=2, reps=5, device="cuda", progress=None):
     nnzb = np.zeros(len(specs), np.int64)
     for k, s in enumerate(specs):
         dt = DType(s.get("dtype", 0))
-        rp, ci = gen_structure(s["M"], s["K"], s["bR"], s["pattern"], s["density"], s["param"], seed=s["seed"])
+        if gpu_structures:
+            from .bcsr import gpu_gen_structure
+            rpd, cid = gpu_gen_structure(s["M"], s["K"], s["bR"], s["pattern"], s["density"], s["param"],
+                                         seed=s["seed"], device=device)
+            rp, ci = rpd.cpu().numpy(), cid.cpu().numpy()
+        else:
+            rp, ci = gen_structure(s["M"], s["K"], s["bR"], s["pattern"], s["density"], s["param"], seed=s["seed"])
+            rpd, cid = torch.as_tensor(rp).to(device), torch.as_tensor(ci).to(device)
         nvals = len(ci) * s["bR"] * 16
         if nvals > pool.numel():
             raise ValueError("value pool too small")
-        rpd, cid = torch.as_tensor(rp).to(device), torch.as_tensor(ci).to(device)
         KN = s["K"] * s["N"]
         B_lo = None
         if dt == DType.E4M3:

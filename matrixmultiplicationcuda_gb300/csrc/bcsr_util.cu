@@ -288,6 +288,13 @@ unsigned grid_for(size_t n) {
 }
 
 }  // namespace
+
+spmm_status scan_counts(const int* counts, int* row_ptr, int n, cudaStream_t s) {
+  k_scan_counts<<<1, 1024, 0, s>>>(counts, row_ptr, n);
+  SPMM_CUDA_TRY(cudaGetLastError());
+  return SPMM_OK;
+}
+
 }  // namespace spmm
 
 using namespace spmm;

@@ -93,4 +93,7 @@ int mma_default_nt(int bR, spmm_dtype dtype, int N);   // the column tile spmm_b
 
 unsigned long long wait_limit_ns();              // bounded-wait limit for device waits
 
+// row_ptr[0] = 0, row_ptr[i + 1] = counts[0] + ... + counts[i] (one CTA, asynchronous).
+spmm_status scan_counts(const int* counts, int* row_ptr, int n, cudaStream_t s);
+
 }  // namespace spmm
