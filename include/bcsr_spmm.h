@@ -225,6 +225,12 @@ typedef struct spmm_csr_desc {
 spmm_status spmm_hcsr_mm(const spmm_bcsr_desc* A_blocks, const spmm_csr_desc* A_rest,
                          const spmm_dense_desc* B, int N, float* C, int ldc,
                          const spmm_config* cfg, void* stream);
+/* CSR x dense (fp16 A and B, fp32 C), the comparator beside the BCSR path. It
+ * replaces the reference's scalar CSR kernel (src/cuda_kernels.cu:271-299, one
+ * thread per output element) with one warp per row and 256 columns. N % 8 == 0,
+ * B and C 16-byte aligned. Asynchronous. */
+spmm_status spmm_csr_mm(const spmm_csr_desc* A, const spmm_dense_desc* B, int N, float* C, int ldc,
+                        void* stream);
 
 /* ---- tuning ----------------------------------------------------------------------
  * No counterpart in the reference (its harness sweeps kernels by hand).

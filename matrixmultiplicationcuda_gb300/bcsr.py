@@ -122,6 +122,25 @@ def hcsr_mm(A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, B, N=None, C=Non
     return C
 
 
+def csr_mm(row_ptr, col_idx, vals, K, B, N=None, C=None, stream=None, ldc=None):
+    """CSR x dense (fp16, device tensors), C fp32: the native comparator."""
+    from ._lib import CsrDesc
+    torch = _torch()
+    N = int(B.shape[1]) if N is None else int(N)
+    M = row_ptr.numel() - 1
+    if C is None:
+        C = torch.empty((M, N), dtype=torch.float32, device=B.device)
+    r = CsrDesc()
+    r.M, r.K = M, int(K)
+    r.row_ptr = row_ptr.data_ptr()
+    r.col_idx = col_idx.data_ptr() if col_idx.numel() else None
+    r.vals = vals.data_ptr() if vals.numel() else None
+    b = _dense_desc(B, None, 1.0, ldb=B.stride(0))
+    check(lib().spmm_csr_mm(ctypes.byref(r), ctypes.byref(b), N, ctypes.c_void_p(C.data_ptr()),
+                            int(C.stride(0)) if ldc is None else int(ldc), stream_handle(stream)))
+    return C
+
+
 def _ref_launch(fn, hdr, idx, data, B, C, M, N, K, stream, extra=()):
     st = fn(_ptr(hdr), _ptr(idx), _ptr(data), _ptr(B), _ptr(C), int(M), int(N), *extra, int(K),
             stream_handle(stream))

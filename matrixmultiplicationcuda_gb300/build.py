@@ -97,7 +97,7 @@ def build_tools(verbose=False):
         deps = [src, LIB] + [os.path.join(ROOT, "include", h) for h in os.listdir(os.path.join(ROOT, "include"))]
         if not (os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps)):
             cmd = [NVCC] + ARCH + ["-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src, "-o", exe + ".tmp",
-                                   "-L" + OUT, "-lbcsr_spmm", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+                                   "-L" + OUT, "-lbcsr_spmm", "-lcublas", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))

@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include "csr.cuh"
 #include "internal.h"
 #include "ptx.cuh"
 #include "spmm_mma.cuh"
@@ -379,20 +380,25 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   } else if (warp >= 4 && warp < 8) {
     // ------------------------------ epilogue (warps 4-7) ---------------------------
     const int q4 = warp & 3;                // TMEM lane quarter this warp may access
+    const bool hybrid = p.csr_row_ptr != nullptr;
     for (uint32_t it = 0;; ++it) {
       int item = -1, start = 0, end = 0, ok = 1;
       if (lane == 0) ok = read_item(it, &item, &start, &end, 16u) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       item = __shfl_sync(0xffffffffu, item, 0);
       const bool empty = __shfl_sync(0xffffffffu, start == end ? 1 : 0, 0) != 0;
-      if (!ok || item < 0) break;
-      const int br = item / (p.ntiles * p.split), nt = (item / p.split) % p.ntiles;
-      const uint32_t acc = it % ACC;
-      if (!mbar_wait(tfull0 + 8 * acc, (it / ACC) & 1, p.timeout_ns)) {
+      bool leave = !ok || item < 0;
+      if (!leave && !mbar_wait(tfull0 + 8 * (it % ACC), (it / ACC) & 1, p.timeout_ns)) {
         if (lane == 0) atomicOr(p.err, 16u);
-        break;
+        leave = true;
       }
+      // The hybrid pass below synchronises the four epilogue warps, so they
+      // agree on leaving (a reduction over the same named barrier) and no warp
+      // is left waiting for one that has gone.
+      if (hybrid ? bar_red_or(1, 128, leave) : leave) break;
       tc_fence_after();
+      const uint32_t acc = (it % ACC);
+      const int br = item / (p.ntiles * p.split), nt = (item / p.split) % p.ntiles;
       const long long row0 = (long long)br * BR;
 #pragma unroll 1
       for (int j = 0; j < Cfg::kJ; ++j) {
@@ -408,21 +414,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 #pragma unroll
             for (int i = 0; i < 16; ++i) v[i] = 0.f;
           }
-          if (p.csr_row_ptr && n < p.N) {
-            // the CSR part of these 16 rows: every entry (r, k, a) adds
-            // a * B[k][n] (one B row per entry, read across the lanes)
-#pragma unroll 1
-            for (int i = 0; i < 16; ++i) {
-              const long long r = row0 + c0 + i;
-              const int e1 = __ldg(p.csr_row_ptr + r + 1);
-              for (int e = __ldg(p.csr_row_ptr + r); e < e1; ++e) {
-                const float a = __half2float(p.csr_vals[e]);
-                v[i] = fmaf(a, __half2float(p.Bh[(long long)__ldg(p.csr_col_idx + e) * p.ldb + n]), v[i]);
-              }
-            }
-          }
           if (n < p.N) {
-            if (p.split == 1) {
+            if (hybrid) {
+              // read back by the CSR pass below: keep the lines in L2
+#pragma unroll
+              for (int i = 0; i < 16; ++i) cptr[(long long)(c0 + i) * p.ldc] = v[i];
+            } else if (p.split == 1) {
 #pragma unroll
               for (int i = 0; i < 16; ++i) __stcs(cptr + (long long)(c0 + i) * p.ldc, v[i]);
             } else if (!empty) {
@@ -435,6 +432,15 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty0 + 8 * acc);
+      if (hybrid) {
+        // The accumulator is free for the next item's MMAs; the CSR part of
+        // this tile's rows is added to C in place. Each CTA owns its C tile
+        // (no split-K here), and the named barrier orders the four warps'
+        // stores above before any lane reads them back.
+        bar_sync_named(1, 128);
+        csr_tile_pass(p.csr_row_ptr, p.csr_col_idx, p.csr_vals, p.Bh, p.ldb, p.C, p.ldc, row0, BR,
+                      nt * NT, min(nt * NT + NT, p.N), q4, lane);
+      }
     }
   }
 

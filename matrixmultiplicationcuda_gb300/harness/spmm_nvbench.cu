@@ -14,7 +14,7 @@
 // algorithmic GB/s, and the fraction of the roofline
 //   t_roof = max(FLOPs / tensor peak, compulsory bytes / HBM peak).
 //
-//   spmm_nvbench [--preset c1|c2|c3|c4|launch|all] [--tuning default,model,sweep]
+//   spmm_nvbench [--preset c1|c2|c3|c4|launch|compare|hybrid|all] [--tuning default,model,sweep]
 //                [--min-samples 20] [--min-time 0.2] [--max-time 2]
 //                [--csv FILE] [--json FILE] [--model FILE] [--peaks FILE]
 //                [--filter SUBSTRING] [--no-check]
@@ -35,9 +35,13 @@
 //       against 64 sequential launches, eager and graph-captured.
 //   launch  host time per call and back-to-back launch rate (L2 warm) on the
 //       c1 and c3 products (not part of "all").
+//   compare the same product as BCSR, CSR (native kernel), dense through the
+//       BCSR pipeline with every block stored, and cuBLAS GemmEx.
+//   hybrid  the hybrid BCSR + CSR product across density thresholds.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <unistd.h>
 
@@ -165,6 +169,7 @@ struct DeviceProduct {
   float* C = nullptr;
   long long nnzb = 0, cols_touched = 0;
   std::vector<int> rp, ci;
+  std::vector<float> host_vals;   // the fp32 block values the product was built from
   std::vector<void*> owned;
   ~DeviceProduct() {
     for (void* p : owned) cudaFree(p);
@@ -259,6 +264,7 @@ void build_product(const Spec& s, DeviceProduct& P) {
   P.B.ldb = s.N;
   P.N = s.N;
   P.C = P.alloc<float>((size_t)s.M * s.N * 4);
+  P.host_vals = std::move(vals);
 }
 
 // Value of stored element i of a quantised array as the GPU reads it.
@@ -563,6 +569,157 @@ class Runner {
     std::fflush(stdout);
   }
 
+  // The same product as BCSR (cost-model configuration), as CSR (the native
+  // CSR kernel), and densely: the BCSR pipeline with every block stored, and
+  // cuBLAS GemmEx (fp16 in, fp32 out) as the library reference point.
+  void compare_bench(const Spec& spec, const char* label) {
+    DeviceProduct P;
+    build_product(spec, P);
+    const int M = spec.M, K = spec.K, N = spec.N, bR = spec.bR;
+    // host CSR of the stored fp16 values, columns ascending
+    std::vector<int> crp(M + 1, 0), cci;
+    std::vector<__half> cv;
+    for (int br = 0; br < M / bR; ++br)
+      for (int r = 0; r < bR; ++r) {
+        for (int j = P.rp[br]; j < P.rp[br + 1]; ++j)
+          for (int c = 0; c < 16; ++c) {
+            const __half h = __float2half(P.host_vals[((size_t)j * bR + r) * 16 + c]);
+            if (__half2float(h) != 0.f) {
+              cci.push_back(P.ci[j] * 16 + c);
+              cv.push_back(h);
+            }
+          }
+        crp[br * bR + r + 1] = (int)cci.size();
+      }
+    int* d_crp = P.alloc<int>(sizeof(int) * (M + 1));
+    int* d_cci = P.alloc<int>(sizeof(int) * std::max<size_t>(cci.size(), 1));
+    __half* d_cv = P.alloc<__half>(2 * std::max<size_t>(cv.size(), 1));
+    CK(cudaMemcpy(d_crp, crp.data(), sizeof(int) * (M + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_cci, cci.data(), sizeof(int) * cci.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_cv, cv.data(), 2 * cv.size(), cudaMemcpyHostToDevice));
+    spmm_csr_desc R{M, K, d_crp, d_cci, d_cv};
+    // the whole matrix, densely: fp16 M x K, and as BCSR with every block stored
+    std::vector<__half> dense((size_t)M * K, __float2half(0.f));
+    for (int br = 0; br < M / bR; ++br)
+      for (int j = P.rp[br]; j < P.rp[br + 1]; ++j)
+        for (int r = 0; r < bR; ++r)
+          for (int c = 0; c < 16; ++c)
+            dense[(size_t)(br * bR + r) * K + P.ci[j] * 16 + c] = __float2half(P.host_vals[((size_t)j * bR + r) * 16 + c]);
+    __half* d_dense = P.alloc<__half>(dense.size() * 2);
+    CK(cudaMemcpy(d_dense, dense.data(), dense.size() * 2, cudaMemcpyHostToDevice));
+    const int MB = M / bR, KB = K / 16;
+    std::vector<int> frp(MB + 1), fci((size_t)MB * KB);
+    std::vector<__half> fv((size_t)M * K);
+    for (int br = 0; br < MB; ++br) {
+      frp[br] = br * KB;
+      for (int j = 0; j < KB; ++j) {
+        fci[(size_t)br * KB + j] = j;
+        for (int r = 0; r < bR; ++r)
+          std::memcpy(&fv[(((size_t)br * KB + j) * bR + r) * 16], &dense[(size_t)(br * bR + r) * K + j * 16], 32);
+      }
+    }
+    frp[MB] = MB * KB;
+    int* d_frp = P.alloc<int>(sizeof(int) * (MB + 1));
+    int* d_fci = P.alloc<int>(sizeof(int) * fci.size());
+    __half* d_fv = P.alloc<__half>(fv.size() * 2);
+    CK(cudaMemcpy(d_frp, frp.data(), sizeof(int) * (MB + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_fci, fci.data(), sizeof(int) * fci.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_fv, fv.data(), fv.size() * 2, cudaMemcpyHostToDevice));
+    spmm_bcsr_desc F = P.A;
+    F.row_ptr = d_frp;
+    F.col_idx = d_fci;
+    F.vals = d_fv;
+    spmm_config cs{}, cf{};
+    const spmm_config* pcs = nullptr;
+    const spmm_config* pcf = nullptr;
+    if (model_) {
+      SK(spmm_cost_model_select(model_, &P.A, N, &cs, nullptr, nullptr));
+      SK(spmm_cost_model_select(model_, &F, N, &cf, nullptr, nullptr));
+      pcs = &cs;
+      pcf = &cf;
+    }
+    cublasHandle_t hb;
+    if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) std::exit(5);
+    const float one = 1.f, zero = 0.f;
+    struct V {
+      std::string name;
+      Sample s;
+    };
+    std::vector<V> v;
+    v.push_back({"BCSR " + config_name(pcs), timer_.measure([&] { SK(spmm_bcsr_mm(&P.A, &P.B, N, P.C, N, pcs, nullptr)); }, o_)});
+    v.push_back({"CSR (native kernel)", timer_.measure([&] { SK(spmm_csr_mm(&R, &P.B, N, P.C, N, nullptr)); }, o_)});
+    v.push_back({"dense: BCSR pipeline, all blocks, " + config_name(pcf),
+                 timer_.measure([&] { SK(spmm_bcsr_mm(&F, &P.B, N, P.C, N, pcf, nullptr)); }, o_)});
+    v.push_back({"dense: cuBLAS GemmEx (library)", timer_.measure([&] {
+                   cublasGemmEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, M, K, &one, P.B.data, CUDA_R_16F, N, d_dense,
+                                CUDA_R_16F, K, &zero, P.C, CUDA_R_32F, N, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+                 }, o_)});
+    SK(spmm_device_error_check(nullptr));
+    cublasDestroy(hb);
+    const double useful = 2.0 * P.nnzb * bR * 16 * N, dense_fl = 2.0 * M * K * N;
+    std::printf("\n## compare: %s (nnzb %lld, CSR nnz %zu)\n\n", label, P.nnzb, cci.size());
+    std::printf("| method | Samples | GPU Time (mean) | Noise | TFLOP/s (nonzero blocks) | dense-equivalent TFLOP/s |\n");
+    std::printf("|---|---|---|---|---|---|\n");
+    for (auto& x : v)
+      std::printf("| %s | %d | %.2f us | %.2f%% | %.1f | %.1f |\n", x.name.c_str(), x.s.samples, x.s.mean_us,
+                  100 * x.s.noise, useful / (x.s.mean_us * 1e-6) / 1e12, dense_fl / (x.s.mean_us * 1e-6) / 1e12);
+    std::fflush(stdout);
+  }
+
+  // The hybrid product across thresholds, as the reference's CLI sweeps them
+  // (main.cu:567-590), on a matrix with dense blocks and scattered entries.
+  void hybrid_bench() {
+    const int M = 4096, K = 4096, N = 1024;
+    std::vector<float> blocks((size_t)M * K), scatter((size_t)M * K), B((size_t)K * N);
+    if (spmm_generate_matrix(M, K, 0.9, "blockrandom", 16, 7u, blocks.data()) != 0 ||
+        spmm_generate_matrix(M, K, 0.98, "random", 16, 8u, scatter.data()) != 0)
+      std::exit(4);
+    std::vector<__half> A((size_t)M * K);
+    for (size_t i = 0; i < A.size(); ++i) A[i] = __float2half(blocks[i] != 0.f ? blocks[i] : scatter[i]);
+    spmm_gen_dense((long long)B.size(), 0, 9, B.data());
+    std::vector<__half> Bh(B.size());
+    for (size_t i = 0; i < B.size(); ++i) Bh[i] = __float2half(B[i]);
+    DeviceProduct P;
+    __half* dB = P.alloc<__half>(Bh.size() * 2);
+    float* dC = P.alloc<float>((size_t)M * N * 4);
+    CK(cudaMemcpy(dB, Bh.data(), Bh.size() * 2, cudaMemcpyHostToDevice));
+    spmm_dense_desc Bd{dB, nullptr, 1.f, N};
+    std::printf("\n## hybrid: A %dx%d (10%% dense 16x16 blocks + 2%% scattered entries), N %d, fp16\n\n", M, K, N);
+    std::printf("| threshold | BCSR blocks | CSR entries | Samples | GPU Time (mean) | Noise | TFLOP/s (stored entries) |\n");
+    std::printf("|---|---|---|---|---|---|---|\n");
+    for (float th : {0.0f, 0.2f, 0.4f, 0.6f, 0.8f, 1.1f}) {
+      long long nnzb = 0, nnz = 0;
+      if (spmm_host_dense_to_hcsr(A.data(), M, K, th, &nnzb, &nnz, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                  nullptr) != 0)
+        std::exit(4);
+      std::vector<int> bh(M / 16 + 1), bi(std::max(nnzb, 1LL)), ch(M + 1), cx(std::max(nnz, 1LL));
+      std::vector<__half> bd(std::max(nnzb, 1LL) * 256), cd(std::max(nnz, 1LL));
+      spmm_host_dense_to_hcsr(A.data(), M, K, th, &nnzb, &nnz, bh.data(), bi.data(), bd.data(), ch.data(), cx.data(),
+                              cd.data());
+      DeviceProduct Q;
+      int* d_bh = Q.alloc<int>(4 * bh.size());
+      int* d_bi = Q.alloc<int>(4 * bi.size());
+      __half* d_bd = Q.alloc<__half>(2 * bd.size());
+      int* d_ch = Q.alloc<int>(4 * ch.size());
+      int* d_cx = Q.alloc<int>(4 * cx.size());
+      __half* d_cd = Q.alloc<__half>(2 * cd.size());
+      CK(cudaMemcpy(d_bh, bh.data(), 4 * bh.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_bi, bi.data(), 4 * bi.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_bd, bd.data(), 2 * bd.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_ch, ch.data(), 4 * ch.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_cx, cx.data(), 4 * cx.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_cd, cd.data(), 2 * cd.size(), cudaMemcpyHostToDevice));
+      spmm_bcsr_desc Ab{M, K, 16, 16, d_bh, d_bi, d_bd, nullptr, nullptr, SPMM_F16};
+      spmm_csr_desc R{M, K, d_ch, d_cx, d_cd};
+      Sample sm = timer_.measure([&] { SK(spmm_hcsr_mm(&Ab, &R, &Bd, N, dC, N, nullptr, nullptr)); }, o_);
+      SK(spmm_device_error_check(nullptr));
+      const double fl = 2.0 * ((double)nnzb * 256 + nnz) * N;
+      std::printf("| %.1f | %lld | %lld | %d | %.2f us | %.2f%% | %.1f |\n", th, nnzb, nnz, sm.samples, sm.mean_us,
+                  100 * sm.noise, fl / (sm.mean_us * 1e-6) / 1e12);
+      std::fflush(stdout);
+    }
+  }
+
   void header(const char* title) {
     std::printf("\n## %s\n\n", title);
     std::printf("| M | N | bR | pattern | density | dtype | tuning | config | Samples | GPU Time (mean) | Noise | "
@@ -721,6 +878,15 @@ int main(int argc, char** argv) {
       }
     } else if (p == "c4") {
       run.batched_bench();
+    } else if (p == "compare") {
+      run.compare_bench(Spec{"compare", 1024, 1024, 1024, 16, 4, 0.10, 0.0, 0, 0, SPMM_F16, 123},
+                        "A 1024^2, 16x16 blocks, reference blockrandom 10 %, N 1024");
+      run.compare_bench(Spec{"compare", 8192, 8192, 1024, 16, 0, 0.05, 0.0, 0, 0, SPMM_F16, 77},
+                        "A 8192^2, 16x16 blocks, random 5 %, N 1024");
+      run.compare_bench(Spec{"compare", 16384, 16384, 512, 64, 0, 0.02, 0.0, 1, 2, SPMM_F16, 20240},
+                        "A 16384^2, 64x16 blocks, random 2 %, N 512");
+    } else if (p == "hybrid") {
+      run.hybrid_bench();
     } else if (p == "launch") {
       std::printf("\n## launch: host time per spmm_bcsr_mm call, back-to-back launches (L2 warm)\n\n");
       std::printf("| product | PDL | host per call | GPU per launch | TFLOP/s |\n|---|---|---|---|---|\n");

@@ -68,3 +68,19 @@ def test_hybrid_rejects_unsupported(dev):
     with pytest.raises(m.SpmmError) as e:
         run_hybrid(dev, A, 0.5, 128, cfg=m.Config(kernel=1))
     assert e.value.status == m.Status.UNSUPPORTED
+
+
+@pytest.mark.parametrize("N", [8, 64, 264, 1024])
+def test_csr_comparator_matches_fp64(dev, N):
+    """The native CSR product on the CSR part of a hybrid split (all entries
+    when the threshold is above 1)."""
+    A = mixed_matrix(384, 512, seed=N)
+    (_, _, _), (ch, cx, cd) = m.host_dense_to_hcsr(A, 1.1)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    B = t(np.random.default_rng(N).uniform(-1, 1, (512, N)).astype(np.float32)).half()
+    C = torch.full((384, N), float("nan"), dtype=torch.float32, device=dev)
+    m.csr_mm(t(ch), t(cx), t(cd.view(np.float16)), 512, B, C=C)
+    m.device_error_check()
+    ref = oracle.f16_to_f32(A).astype(np.float64) @ B.cpu().double().numpy()
+    mx, fr = oracle.rel_errors(C.cpu().numpy(), ref)
+    assert mx <= 1e-5 and fr <= 1e-5
