@@ -445,11 +445,15 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     sampler.mark("timed_start")
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # NVTX range "bench_timed": a profiler can capture exactly the timed launches
+    # (ncu --nvtx --nvtx-include "bench_timed/")
+    torch.cuda.nvtx.range_push("bench_timed")
     g0.record(stream)
     for i in range(args.steps):
         launch(probs[i % len(probs)], cfg)
     g1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     sampler.mark("timed_end")
     barrier(world)
     m.device_error_check()

@@ -210,8 +210,8 @@ spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
 
 /* ---- hybrid BCSR + CSR (HCSRMatrix, formats/HCSRMatrix.cpp:10-36) -------------
  * C = A_blocks B + A_rest B in ONE launch: the tcgen05 pipeline multiplies the
- * BCSR part (any block height; the reference uses 16 x 16) and its epilogue
- * adds the CSR part's entries of each row before C is stored. The reference
+ * BCSR part (any block height; the reference uses 16 x 16), and its epilogue
+ * warps add the CSR part's entries to each tile after storing it. The reference
  * runs three kernels (CSR into a second buffer, BCSR into C, then an
  * element-wise add; main.cu:567-590). fp16 only, no split-K. Both parts
  * describe the same M x K matrix; A_rest->row_ptr has M + 1 entries, col_idx
@@ -225,6 +225,23 @@ typedef struct spmm_csr_desc {
 spmm_status spmm_hcsr_mm(const spmm_bcsr_desc* A_blocks, const spmm_csr_desc* A_rest,
                          const spmm_dense_desc* B, int N, float* C, int ldc,
                          const spmm_config* cfg, void* stream);
+/* The hybrid product with a plan: the CSR part is packed once into gather
+ * blocks (16 entries of one 16-row block row each, as a 16 x 16 block whose
+ * column c holds entry c, plus the entries' 16 B-row indices). The tcgen05
+ * pipeline then runs stored and gather blocks alike on the tensor cores, and
+ * fetches a gather block's B rows with TMA tile::gather4. 16 x 16 fp16 blocks.
+ * _create reads both parts on the device and synchronises `stream` once (for
+ * the sizes). The plan owns its arrays: the parts may be freed after _create.
+ * _run only launches (one kernel; no allocation or synchronisation); any N,
+ * ldb, ldc, configuration and split-K of kernel 2. */
+typedef struct spmm_hcsr_plan spmm_hcsr_plan;
+spmm_status spmm_hcsr_plan_create(const spmm_bcsr_desc* A_blocks, const spmm_csr_desc* A_rest,
+                                  void* stream, spmm_hcsr_plan** plan_out);
+spmm_status spmm_hcsr_plan_info(const spmm_hcsr_plan* plan, long long* blocks,
+                                long long* gather_blocks);
+spmm_status spmm_hcsr_plan_run(const spmm_hcsr_plan* plan, const spmm_dense_desc* B, int N,
+                               float* C, int ldc, const spmm_config* cfg, void* stream);
+spmm_status spmm_hcsr_plan_destroy(spmm_hcsr_plan* plan);
 /* CSR x dense (fp16 A and B, fp32 C), the comparator beside the BCSR path. It
  * replaces the reference's scalar CSR kernel (src/cuda_kernels.cu:271-299, one
  * thread per output element) with one warp per row and 256 columns. N % 8 == 0,

@@ -38,6 +38,7 @@ from .bcsr import (  # noqa: F401
     debug_wait_timeout,
     BatchPlan,
     hcsr_mm,
+    HcsrPlan,
     csr_mm,
     gpu_gen_structure,
     gpu_gen_values,

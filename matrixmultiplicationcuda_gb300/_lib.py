@@ -77,6 +77,12 @@ _SIGS = {
     "spmm_gpu_gen_dense": (c_int, [c_ll, c_int, c_ull, c_vp, c_vp]),
     "spmm_gpu_generate_matrix": (c_int, [c_int, c_int, c_double, c_char_p, c_int, c_ull, c_vp, c_vp]),
     "spmm_csr_mm": (c_int, [ctypes.POINTER(CsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp, c_int, c_vp]),
+    "spmm_hcsr_plan_create": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(CsrDesc), c_vp,
+                                      ctypes.POINTER(c_vp)]),
+    "spmm_hcsr_plan_info": (c_int, [c_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+    "spmm_hcsr_plan_run": (c_int, [c_vp, ctypes.POINTER(DenseDesc), c_int, c_vp, c_int, ctypes.POINTER(Config),
+                                   c_vp]),
+    "spmm_hcsr_plan_destroy": (c_int, [c_vp]),
     "spmm_hcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(CsrDesc), ctypes.POINTER(DenseDesc), c_int,
                              c_vp, c_int, ctypes.POINTER(Config), c_vp]),
     "sparseMatrixMulTensor_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),

@@ -122,6 +122,53 @@ def hcsr_mm(A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, B, N=None, C=Non
     return C
 
 
+class HcsrPlan:
+    """The planned hybrid product (fp16, 16x16 blocks): the CSR part packed once
+    into gather blocks that the tcgen05 pipeline runs beside the stored blocks.
+    The plan copies both parts; run() is one launch."""
+
+    def __init__(self, A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, stream=None):
+        from ._lib import CsrDesc
+        a = A_blocks.desc()
+        r = CsrDesc()
+        r.M, r.K = A_blocks.M, A_blocks.K
+        r.row_ptr = csr_row_ptr.data_ptr()
+        r.col_idx = csr_col_idx.data_ptr() if csr_col_idx.numel() else None
+        r.vals = csr_vals.data_ptr() if csr_vals.numel() else None
+        self.M, self.K = A_blocks.M, A_blocks.K
+        h = ctypes.c_void_p()
+        check(lib().spmm_hcsr_plan_create(ctypes.byref(a), ctypes.byref(r), stream_handle(stream), ctypes.byref(h)))
+        self._h = h
+
+    def info(self):
+        """(blocks, gather_blocks) of the packed matrix."""
+        nb, ng = ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().spmm_hcsr_plan_info(self._h, ctypes.byref(nb), ctypes.byref(ng)))
+        return nb.value, ng.value
+
+    def run(self, B, N=None, C=None, cfg: Optional[Config] = None, stream=None, ldc=None):
+        torch = _torch()
+        N = int(B.shape[1]) if N is None else int(N)
+        if C is None:
+            C = torch.empty((self.M, N), dtype=torch.float32, device=B.device)
+        ldc = int(C.stride(0)) if ldc is None else int(ldc)
+        b = _dense_desc(B, None, 1.0, ldb=B.stride(0))
+        check(lib().spmm_hcsr_plan_run(self._h, ctypes.byref(b), N, ctypes.c_void_p(C.data_ptr()), ldc,
+                                       ctypes.byref(cfg) if cfg is not None else None, stream_handle(stream)))
+        return C
+
+    def close(self):
+        if self._h:
+            lib().spmm_hcsr_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def csr_mm(row_ptr, col_idx, vals, K, B, N=None, C=None, stream=None, ldc=None):
     """CSR x dense (fp16, device tensors), C fp32: the native comparator."""
     from ._lib import CsrDesc

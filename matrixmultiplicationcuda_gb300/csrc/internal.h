@@ -76,6 +76,11 @@ struct LaunchRequest {
   unsigned* queue = nullptr;
   // hybrid product: the CSR part added by the tcgen05 pipeline's epilogue
   const spmm_csr_desc* csr = nullptr;
+  // planned hybrid product: A holds gather blocks (col_idx = -(g + 1)) whose
+  // 16 B rows are gather_rows[16g .. 16g + 15]; total_blocks counts A's
+  // stored and gather blocks
+  const int* gather_rows = nullptr;
+  long long total_blocks = 0;
 };
 // mma.sync family (spmm_mma.cu)
 spmm_status launch_mma(const LaunchRequest& r);

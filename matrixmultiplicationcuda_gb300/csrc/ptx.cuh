@@ -114,6 +114,18 @@ __device__ __forceinline__ void tma_tile_2d_g2s(uint32_t dst, const void* tmap, 
       "l"(tmap), "r"(x), "r"(y), "r"(bar), "l"(policy)
       : "memory");
 }
+// Four rows y0..y3 of a 2-D tensor, columns [x, x + box width), global -> shared
+// (tile::gather4; the map's box is one row high). The rows land one after the
+// other at dst with the map's swizzle, as rows of one taller box would. A row
+// outside the tensor reads the fill value (zeros).
+__device__ __forceinline__ void tma_gather4_g2s(uint32_t dst, const void* tmap, int x, int y0, int y1, int y2,
+                                                int y3, uint32_t bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+      ".L2::cache_hint [%0], [%1, {%2, %3, %4, %5, %6}], [%7], %8;" ::"r"(dst),
+      "l"(tmap), "r"(x), "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(bar), "l"(policy)
+      : "memory");
+}
 // Tiled 3-D tensor copy global -> shared; {x, y, z} innermost first.
 __device__ __forceinline__ void tma_tile_3d_g2s(uint32_t dst, const void* tmap, int x, int y, int z,
                                                 uint32_t bar, uint64_t policy) {

@@ -62,6 +62,9 @@ struct TcParams {
   const __half* csr_vals;
   const __half* Bh;
   long long ldb;
+  // planned hybrid product: a block with col_idx = -(g + 1) is a gather block,
+  // whose panel rows are B rows gather_rows[16g .. 16g + 15] (NULL: none)
+  const int* gather_rows;
 };
 
 // BR: block height (the UMMA N); NT: output columns per item; STAGES: ring
@@ -302,6 +305,28 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
           for (int b = bidx; b < n; b += kBIssuers) {
             const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
+            if constexpr (!Cfg::kSplit) {
+              if (col < 0 && p.gather_rows) {
+                // Gather block: its panel is 16 arbitrary B rows. Lane L < 4 * (NT / 64)
+                // copies rows 4q .. 4q + 3 (q = L % 4) of 64-column box L / 4 with one
+                // tile::gather4 (tmBlo is then the one-row-box view of B), into the
+                // box's rows 4q .. 4q + 3: the image of a 16-row box copy. Padding
+                // rows index K, past the end of B, and read zeros.
+                const long long g = -(long long)col - 1;
+                const int kk = lane < 16 ? __ldg(p.gather_rows + 16 * g + lane) : 0;
+                const int q = lane & 3;
+                const int y0 = __shfl_sync(0xffffffffu, kk, 4 * q);
+                const int y1 = __shfl_sync(0xffffffffu, kk, 4 * q + 1);
+                const int y2 = __shfl_sync(0xffffffffu, kk, 4 * q + 2);
+                const int y3 = __shfl_sync(0xffffffffu, kk, 4 * q + 3);
+                if (lane < 4 * (NT / 64)) {
+                  const int bx = lane >> 2;
+                  tma_gather4_g2s(smem_u32(b_dst0 + (size_t)b * Cfg::kPanelBytes + bx * Cfg::kBoxBytes + q * 512),
+                                  &tmBlo, nt * NT + bx * 64, y0, y1, y2, y3, full0 + 8 * s, pol_b);
+                }
+                continue;
+              }
+            }
             if (lane == 0) {
               const uint32_t fb = full0 + 8 * s;
               uint8_t* b_dst = b_dst0 + (size_t)b * Cfg::kPanelBytes * Cfg::kParts;
@@ -527,8 +552,10 @@ spmm_status launch_tc(const LaunchRequest& r) {
   // A's values viewed as a [rows x 16] fp16 tensor; rows bounded by the densest
   // possible matrix (only coordinates of stored blocks are ever requested: a
   // group copy is issued only for kGroup consecutive blocks of one block row).
-  const unsigned long long rows_bound =
+  unsigned long long rows_bound =
       std::max<unsigned long long>((unsigned long long)(A.M / A.bR) * (A.K / 16) * A.bR, 256ull);
+  if (r.gather_rows)   // gather blocks come on top of at most K / 16 stored blocks per row
+    rows_bound = std::max<unsigned long long>(rows_bound, (unsigned long long)r.total_blocks * A.bR);
   if (rows_bound >= (1ull << 31)) return fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline");
   CUtensorMap tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo;
   const void* vals = A.vals ? A.vals : B.data;   // no stored blocks: never dereferenced
@@ -552,6 +579,13 @@ spmm_status launch_tc(const LaunchRequest& r) {
   tmAlo1 = tmA1;
   tmAlog = tmAg;
   tmBlo = tmB;
+  if (r.gather_rows) {
+    // gather blocks: tmBlo becomes B viewed with a one-row box, the form tile::gather4 copies
+    if (mode == MODE_SPLIT) return fail(SPMM_ERR_UNSUPPORTED, "gather blocks run in fp16 or bf16");
+    st = encode_tile_map_2d(&tmBlo, CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data, (uint64_t)r.N, (uint64_t)A.K,
+                            (uint64_t)B.ldb * 2, 64, 1, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (st != SPMM_OK) return st;
+  }
   if (mode == MODE_SPLIT) {
     const void* lo = A.vals_lo ? A.vals_lo : B.data_lo;
     st = encode_tile_map_2d(&tmAlo1, CU_TENSOR_MAP_DATA_TYPE_UINT16, lo, 16, rows_bound, 32, 16,
@@ -588,6 +622,7 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.csr_vals = r.csr ? static_cast<const __half*>(r.csr->vals) : nullptr;
   p.Bh = static_cast<const __half*>(B.data);
   p.ldb = B.ldb;
+  p.gather_rows = r.gather_rows;
   if (r.csr && (p.split > 1 || mode != MODE_F16))
     return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product runs in fp16 without split-K");
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");

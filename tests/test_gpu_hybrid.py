@@ -84,3 +84,99 @@ def test_csr_comparator_matches_fp64(dev, N):
     ref = oracle.f16_to_f32(A).astype(np.float64) @ B.cpu().double().numpy()
     mx, fr = oracle.rel_errors(C.cpu().numpy(), ref)
     assert mx <= 1e-5 and fr <= 1e-5
+
+
+def run_plan(dev, A_bits, th, N, seed=1, cfg=None, Bf=None):
+    """The planned hybrid product (gather blocks) on the same split."""
+    M, K = A_bits.shape
+    (bh, bi, bd), (ch, cx, cd) = m.host_dense_to_hcsr(A_bits, th)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    Ab = m.BCSR(M, K, 16, 16, t(bh), t(bi), t(bd.view(np.float16)))
+    if Bf is None:
+        Bf = np.random.default_rng(seed).uniform(-1, 1, (K, N)).astype(np.float32)
+    B = t(Bf).half()
+    plan = m.HcsrPlan(Ab, t(ch), t(cx), t(cd.view(np.float16)))
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    plan.run(B, N=N, C=C, cfg=cfg)
+    m.device_error_check()
+    info = plan.info()
+    plan.close()
+    # the packed matrix: every stored block plus ceil(entries / 16) gather blocks per block row
+    ent = np.diff(ch)[: M].reshape(M // 16, 16).sum(1)
+    assert info == (len(bi) + int(((ent + 15) // 16).sum()), int(((ent + 15) // 16).sum()))
+    Ad = oracle.f16_to_f32(A_bits).astype(np.float64)
+    Bn = B.cpu().double().numpy()
+    # the product over A's entries: a B row that only meets zero columns of A
+    # takes no part (the FP64 product would form 0 * inf there)
+    unused = ~Ad.any(axis=0)
+    Bn[unused] = np.where(np.isfinite(Bn[unused]), Bn[unused], 0.0)
+    ref = Ad @ Bn
+    return C.cpu().numpy(), ref, len(bi), len(cx)
+
+
+@pytest.mark.parametrize("th", [0.0, 0.3, 0.6, 1.1])
+@pytest.mark.parametrize("N", [64, 200, 512])
+def test_hybrid_plan_matches_fp64(dev, th, N):
+    A = mixed_matrix(512, 768, seed=int(th * 10) + N + 7)
+    got, ref, nnzb, nnz = run_plan(dev, A, th, N)
+    assert np.isfinite(got).all()
+    mx, fr = oracle.rel_errors(got, ref)
+    assert mx <= 2e-5 and fr <= 2e-5, (th, nnzb, nnz, mx, fr)
+
+
+@pytest.mark.parametrize("cfg", [dict(n_tile=256, schedule=1), dict(n_tile=512), dict(n_tile=256, split_k=2)])
+def test_hybrid_plan_configurations(dev, cfg):
+    A = mixed_matrix(1024, 1024, seed=11)
+    got, ref, nnzb, nnz = run_plan(dev, A, 0.5, 512, cfg=m.Config(kernel=2, **cfg))
+    assert nnzb > 0 and nnz > 0
+    mx, fr = oracle.rel_errors(got, ref)
+    assert mx <= 2e-5 and fr <= 2e-5
+
+
+def test_hybrid_plan_long_rows_and_empty_parts(dev):
+    """Rows of 1000+ CSR entries (many gather blocks per block row), and the
+    all-zero matrix (no blocks of either kind)."""
+    M, K, N = 64, 4096, 256
+    rng = np.random.default_rng(3)
+    A = np.zeros((M, K), np.float32)
+    A[::16] = rng.uniform(-1, 1, (M // 16, K))          # one full row per block row: density 1/16
+    A[5, ::3] = rng.uniform(-1, 1, len(range(0, K, 3)))
+    bits = oracle.f32_to_f16(A).view(np.uint16).reshape(M, K)
+    got, ref, nnzb, nnz = run_plan(dev, bits, 0.5, N)
+    assert nnzb == 0 and nnz > 4000
+    mx, fr = oracle.rel_errors(got, ref)
+    assert mx <= 2e-5 and fr <= 2e-5
+    zero = np.zeros((M, K), np.uint16)
+    got, ref, nnzb, nnz = run_plan(dev, zero, 0.5, N)
+    assert nnzb == 0 and nnz == 0 and (got == 0).all()
+
+
+def test_hybrid_plan_padding_reads_zeros(dev):
+    """Unused slots of a gather block index row K (past B) and must add exact
+    zeros: B's row 0 is +inf and no entry or stored block of A touches column
+    0, so a slot that read a real row of B would turn C into NaN."""
+    M, K, N = 256, 512, 128
+    A = mixed_matrix(M, K, seed=21).copy()
+    A[:, 0] = 0
+    A[:, :16] &= np.where(np.random.default_rng(2).uniform(size=(M, 16)) < 0.1, 0xFFFF, 0).astype(np.uint16)
+    Bf = np.random.default_rng(4).uniform(-1, 1, (K, N)).astype(np.float32)
+    Bf[0] = np.inf
+    got, ref, nnzb, nnz = run_plan(dev, A, 0.5, N, Bf=Bf)
+    assert nnz > 0 and np.isfinite(got).all()
+    mx, fr = oracle.rel_errors(got, ref)
+    assert mx <= 2e-5 and fr <= 2e-5
+
+
+def test_hybrid_plan_rejects_unsupported(dev):
+    A = mixed_matrix(128, 128, seed=3)
+    with pytest.raises(m.SpmmError) as e:
+        run_plan(dev, A, 0.5, 128, cfg=m.Config(kernel=1))
+    assert e.value.status == m.Status.UNSUPPORTED
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    rp, ci = m.gen_structure(128, 128, 32, m.PATTERN_RANDOM, 0.2, 0, seed=1)
+    vals = m.gen_values(len(ci), 32, 16, m.DIST_UNIFORM, seed=2)
+    A32 = m.BCSR.from_host(128, 128, 32, rp, ci, vals, m.DType.F16, device=dev)
+    z = torch.zeros(129, dtype=torch.int32, device=dev)
+    with pytest.raises(m.SpmmError) as e:
+        m.HcsrPlan(A32, z, z[:0], z[:0].half())
+    assert e.value.status == m.Status.UNSUPPORTED
