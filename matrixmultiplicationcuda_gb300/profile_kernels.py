@@ -13,6 +13,11 @@ Families (seeded synthetic inputs; a few hundred MB on the device at most):
             8192 x 8192 (134 MB) with 16x16 blocks at 5 %
   quantize  k_to_f16 / k_to_bf16 / k_absmax / k_to_e4m3: 64 M fp32 values
   mlp       the cost model's forward / backward / AdamW kernels, batch 2000
+  hybrid    k_bcsr_tc with the CSR pass in its epilogue (spmm_hcsr_mm): A 4096^2
+            (10 % dense 16x16 blocks + 2 % scattered entries), threshold 0.5,
+            N 1024
+  hybrid_plan  the same product planned: CSR entries as gather blocks
+  csr       k_csr_mm on the same matrix's entries, all as CSR
 Each family runs `--launches` times after one warm-up, then synchronises and
 checks the device error word.
 """
@@ -28,7 +33,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp")
+    ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args(argv)
     import torch
@@ -111,6 +116,30 @@ def main(argv=None):
         for dt in (m.DType.F16, m.DType.BF16, m.DType.E4M3):
             run(lambda: m.quantize(src, dt, block_elems=1024))
         print("quantize: %d values" % src.numel())
+    if only & {"hybrid", "hybrid_plan", "csr"}:
+        M = K = 4096
+        N = 1024
+        blocks = m.generate_matrix(M, K, 0.9, "blockrandom", 16, seed=7)
+        scatter = m.generate_matrix(M, K, 0.98, "random", 16, seed=8)
+        A = np.where(blocks != 0, blocks, scatter).astype(np.float16).view(np.uint16)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        B = t(m.gen_dense(K, N, m.DIST_UNIFORM, seed=9)).half()
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        (bh, bi, bd), (ch, cx, cd) = m.host_dense_to_hcsr(A, 0.5)
+        Ab = m.BCSR(M, K, 16, 16, t(bh), t(bi), t(bd.view(np.float16)))
+        if "hybrid" in only:
+            run(lambda: m.hcsr_mm(Ab, t(ch), t(cx), t(cd.view(np.float16)), B, N=N, C=C))
+            print("hybrid: %d blocks, %d CSR entries" % (len(bi), len(cx)))
+        if "hybrid_plan" in only:
+            plan = m.HcsrPlan(Ab, t(ch), t(cx), t(cd.view(np.float16)))
+            run(lambda: plan.run(B, N=N, C=C))
+            print("hybrid_plan: (blocks, gather blocks) =", plan.info())
+            plan.close()
+        if "csr" in only:
+            _, (rh, rx, rd) = m.host_dense_to_hcsr(A, 1.1)
+            rh, rx, rd = t(rh), t(rx), t(rd.view(np.float16))
+            run(lambda: m.csr_mm(rh, rx, rd, K, B, N=N, C=C))
+            print("csr: %d entries" % rx.numel())
     if "mlp" in only:
         s = costmodel.shape()
         rng = np.random.default_rng(0)
