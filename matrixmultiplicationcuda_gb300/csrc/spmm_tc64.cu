@@ -48,7 +48,6 @@ struct Tc64Params {
   unsigned* err;
   int panel3d;
   unsigned* queue;
-  int split;
 };
 
 // NT: output columns per item (256 or 512); STAGES: ring depth in groups;
@@ -158,24 +157,15 @@ __global__ void __launch_bounds__(kTc64Threads, 1)
         int v = p.queue ? (int)atomicAdd(p.queue, 1u) : (cur < 0 ? (int)blockIdx.x : cur + (int)gridDim.x);
         return v < p.n_items ? v : -1;
       };
-      // block range of an item: its block row's range, or one of p.split slices
-      // of it (slice lengths a multiple of 4 blocks)
+      // block range of an item: its block row's range
       auto range = [&](int v, int* s0, int* s1) {
         if (v < 0) {
           *s0 = *s1 = 0;
           return;
         }
-        const int row = v / (p.ntiles * p.split);
-        int a = __ldg(p.row_ptr + row), b = __ldg(p.row_ptr + row + 1);
-        if (p.split > 1) {
-          const int k = v % p.split;
-          const int chunk = (((b - a) + p.split - 1) / p.split + 3) & ~3;
-          const int a2 = min(b, a + k * chunk);
-          b = min(b, a2 + chunk);
-          a = a2;
-        }
-        *s0 = a;
-        *s1 = b;
+        const int row = v / p.ntiles;
+        *s0 = __ldg(p.row_ptr + row);
+        *s1 = __ldg(p.row_ptr + row + 1);
       };
       uint32_t gs = 0, it = 0;
       bool failed = false;
@@ -249,7 +239,7 @@ __global__ void __launch_bounds__(kTc64Threads, 1)
       start = __shfl_sync(0xffffffffu, start, 0);
       end = __shfl_sync(0xffffffffu, end, 0);
       if (!ok || item < 0) break;
-      const int nt = (item / p.split) % p.ntiles;
+      const int nt = item % p.ntiles;
       int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
@@ -518,8 +508,7 @@ spmm_status launch_tc64(const LaunchRequest& r) {
   p.N = r.N;
   p.ntiles = (r.N + nt - 1) / nt;
   if (r.cfg.split_k > 1) return fail(SPMM_ERR_UNSUPPORTED, "the 64-row pipeline has no split-K");
-  p.split = 1;
-  const long long n_items = (long long)(A.M / 64) * p.ntiles * p.split;
+  const long long n_items = (long long)(A.M / 64) * p.ntiles;
   if (n_items >= (1ll << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
   p.n_items = (int)n_items;
   p.timeout_ns = wait_limit_ns();
@@ -528,8 +517,6 @@ spmm_status launch_tc64(const LaunchRequest& r) {
   p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");
   if (p.n_items == 0) return SPMM_OK;
-  if (p.split > 1)
-    SPMM_CUDA_TRY(cudaMemset2DAsync(r.C, (size_t)r.ldc * 4, 0, (size_t)r.N * 4, A.M, r.stream));
   SPMM_CUDA_TRY(ensure_smem_attr(reinterpret_cast<const void*>(e->fn), (int)e->smem));
   long long grid = sm_count();
   if (grid > p.n_items) grid = p.n_items;
