@@ -86,6 +86,38 @@ def test_csr_comparator_matches_fp64(dev, N):
     assert mx <= 1e-5 and fr <= 1e-5
 
 
+def test_csr_comparator_ragged_rows_and_checks(dev):
+    """M not a multiple of the kernel's 8 rows per CTA, empty rows (every row
+    of C is written, zeros there), a leading dimension above N, and the
+    argument checks (N % 8, unaligned B)."""
+    M, K, N = 101, 96, 40
+    rng = np.random.default_rng(5)
+    A = (rng.uniform(-1, 1, (M, K)) * (rng.uniform(size=(M, K)) < 0.1)).astype(np.float32)
+    A[3] = 0
+    A[50:60] = 0
+    bits = oracle.f32_to_f16(A).view(np.uint16).reshape(M, K)
+    ch, cx, cd = m.host_dense_to_csr(bits)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    B = t(rng.uniform(-1, 1, (K, N)).astype(np.float32)).half()
+    Cbig = torch.full((M, 48), float("nan"), dtype=torch.float32, device=dev)
+    m.csr_mm(t(ch), t(cx), t(cd.view(np.float16)), K, B, C=Cbig, ldc=48)
+    m.device_error_check()
+    got = Cbig[:, :N].cpu().numpy()
+    ref = oracle.f16_to_f32(bits).astype(np.float64) @ B.cpu().double().numpy()
+    assert (got[3] == 0).all() and (got[50:60] == 0).all()
+    assert np.isnan(Cbig[:, N:].cpu().numpy()).all()     # columns past N untouched
+    mx, fr = oracle.rel_errors(got, ref)
+    assert mx <= 1e-5 and fr <= 1e-5
+    with pytest.raises(m.SpmmError) as e:
+        m.csr_mm(t(ch), t(cx), t(cd.view(np.float16)), K, B[:, :36], N=36)
+    assert e.value.status == m.Status.UNSUPPORTED
+    Bbuf = torch.zeros(K * N + 8, dtype=torch.float16, device=dev)
+    Bmis = Bbuf[4:4 + K * N].view(K, N)                   # 8 bytes off a 16-byte boundary
+    with pytest.raises(m.SpmmError) as e:
+        m.csr_mm(t(ch), t(cx), t(cd.view(np.float16)), K, Bmis)
+    assert e.value.status == m.Status.MISALIGNED
+
+
 def run_plan(dev, A_bits, th, N, seed=1, cfg=None, Bf=None):
     """The planned hybrid product (gather blocks) on the same split."""
     M, K = A_bits.shape
