@@ -18,6 +18,11 @@ Families (seeded synthetic inputs; a few hundred MB on the device at most):
             N 1024
   hybrid_plan  the same product planned: CSR entries as gather blocks
   csr       k_csr_mm on the same matrix's entries, all as CSR
+  tc64      k_bcsr_tc64 (64-row blocks, M=64 UMMAs, one CTA per SM): the tc
+            product in fp16 and in split fp16, 256-column tile
+  gen       the GPU generators: k_gen_structure + k_gen_values for the tc
+            product's structure (A 16384^2, 64x16, 2 %), k_gen_dense for B
+            (16384 x 512), k_gen_matrix (reference blockrandom, 8192^2 fp16)
 Each family runs `--launches` times after one warm-up, then synchronises and
 checks the device error word.
 """
@@ -33,7 +38,8 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr")
+    ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr,"
+                                      "tc64,gen")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args(argv)
     import torch
@@ -140,6 +146,20 @@ def main(argv=None):
             rh, rx, rd = t(rh), t(rx), t(rd.view(np.float16))
             run(lambda: m.csr_mm(rh, rx, rd, K, B, N=N, C=C))
             print("csr: %d entries" % rx.numel())
+    if "tc64" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256)))
+        A, B, Blo, bs, C = c3(m.DType.F16_SPLIT)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256), B_lo=Blo))
+        print("tc64: nnzb=%d" % A.nnzb)
+    if "gen" in only:
+        def gen():
+            rp, ci = m.gpu_gen_structure(16384, 16384, 64, m.PATTERN_RANDOM, 0.02, 0, seed=20240, device=dev)
+            m.gpu_gen_values(ci.numel(), 64, 16, m.DIST_SCALED_NORMAL, seed=20241, device=dev)
+            m.gpu_gen_dense(16384, 512, m.DIST_NORMAL, seed=20242, device=dev)
+            m.gpu_generate_matrix(8192, 8192, 0.9, "blockrandom", 16, seed=7, device=dev)
+        run(gen)
+        print("gen: done")
     if "mlp" in only:
         s = costmodel.shape()
         rng = np.random.default_rng(0)
