@@ -519,7 +519,7 @@ def run_ours(args, world, rank, local):
     batched = None if args.no_batch else bench_batched(m, torch, dev, flush, hbm_peak)
 
     # CPU baseline (reference host multiply, restated), rank 0 only, bounded sample
-    cpu = None
+    cpu = cpu_sparse = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         vh = vals.astype(np.float16).astype(np.float32)
         Bh = Bf.astype(np.float16).view(np.uint16)
@@ -527,6 +527,22 @@ def run_ours(args, world, rank, local):
         cpu = {"value": rate, "unit": "TFLOP/s", "cores": 1, "kind": "port",
                "sample": "192 of %d output rows, reference host multiply (dense i-k-j, fp32, "
                          "one thread), repeated for %.1f s" % (M, secs)}
+        # beside it, a block-sparse fp32 host multiply on every host core: a
+        # baseline only, not the reference's algorithm
+        from oracle import oracle
+        threads = os.cpu_count() or 1
+        vbits = vals.astype(np.float16).view(np.uint16)
+        Bq = Bf.astype(np.float16).astype(np.float32).reshape(K, N)
+        t0, runs = time.perf_counter(), 0
+        while True:
+            oracle.bcsr_matmul_f32_mt(rp, ci, vbits, BR, Bq, threads=threads)
+            runs += 1
+            if time.perf_counter() - t0 >= 3.0:
+                break
+        secs_s = time.perf_counter() - t0
+        cpu_sparse = {"value": runs * flops / secs_s / 1e12, "unit": "TFLOP/s", "cores": threads,
+                      "kind": "block-sparse host multiply (baseline only)",
+                      "sample": "the whole product, %d runs in %.1f s, fp32, split by block rows" % (runs, secs_s)}
 
     tr = results[tuned]
     bytes_launch = tr["bytes"]
@@ -561,6 +577,7 @@ def run_ours(args, world, rank, local):
                          "algorithmic_bytes": bytes_launch, "peak_source": peak_kind,
                          "tensor_frac": (flops / (kern_ms * 1e-3) / 1e12) / tensor_peak},
             "cpu_baseline": cpu,
+            "cpu_baseline_block_sparse": cpu_sparse,
             "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": args.steps,

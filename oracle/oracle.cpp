@@ -248,6 +248,46 @@ void oracle_cpu_matmul_ref_rows_mt(const uint16_t* A, const uint16_t* B, int M, 
   for (auto& x : th) x.join();
 }
 
+// Block-sparse host multiply, a CPU baseline only (not a reference algorithm):
+// C = A (BCSR, fp16 bits) x B (fp32, K x N), fp32 accumulation, over block rows
+// [br0, br1), split across nthreads threads by block row. Each stored block
+// adds a * B[k][:] into its rows, so only the stored blocks' MACs are done.
+// C holds (br1 - br0) * bR rows of N.
+void oracle_bcsr_matmul_f32_mt(const int* row_ptr, const int* col_idx, const uint16_t* vals, int bR,
+                               const float* B, int K, int N, int br0, int br1, float* C, int nthreads) {
+  (void)K;
+  auto rows = [&](int a0, int a1) {
+    for (int br = a0; br < a1; ++br) {
+      float* c = C + (size_t)(br - br0) * bR * N;
+      std::fill(c, c + (size_t)bR * N, 0.0f);
+      for (int k = row_ptr[br]; k < row_ptr[br + 1]; ++k) {
+        const uint16_t* a = vals + (size_t)k * bR * 16;
+        const float* b = B + (size_t)col_idx[k] * 16 * N;
+        for (int x = 0; x < bR; ++x) {
+          float* crow = c + (size_t)x * N;
+          for (int y = 0; y < 16; ++y) {
+            const float av = f16_to_f32(a[x * 16 + y]);
+            if (av == 0.0f) continue;
+            const float* brow = b + (size_t)y * N;
+            for (int j = 0; j < N; ++j) crow[j] += av * brow[j];
+          }
+        }
+      }
+    }
+  };
+  if (nthreads <= 1) {
+    rows(br0, br1);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int n = br1 - br0;
+  for (int t = 0; t < nthreads; ++t) {
+    const int a = br0 + (int)((long long)n * t / nthreads), b = br0 + (int)((long long)n * (t + 1) / nthreads);
+    if (a < b) th.emplace_back(rows, a, b);
+  }
+  for (auto& x : th) x.join();
+}
+
 // FP64 BCSR x dense product, the error reference for every precision.
 // A is given by its BCSR structure and block values in double (the exact
 // values before any storage rounding), B as double, row-major ld = N.

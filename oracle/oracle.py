@@ -46,6 +46,8 @@ def lib():
         L.oracle_bcsr_fill.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
         L.oracle_cpu_matmul_ref_rows.argtypes = [P, P] + [ctypes.c_int] * 5 + [P]
         L.oracle_cpu_matmul_ref_rows_mt.argtypes = [P, P] + [ctypes.c_int] * 5 + [P, ctypes.c_int]
+        L.oracle_bcsr_matmul_f32_mt.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
         L.oracle_bcsr_matmul_f64.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, P]
         L.oracle_maxdiff.restype = ctypes.c_float
@@ -130,6 +132,20 @@ def cpu_matmul_ref(A_bits, B_bits, row0=0, row1=None, threads=1):
     row1 = M if row1 is None else row1
     C = np.empty((row1 - row0, N), np.float32)
     lib().oracle_cpu_matmul_ref_rows_mt(_p(A), _p(B), M, K, N, row0, row1, _p(C), int(threads))
+    return C
+
+
+def bcsr_matmul_f32_mt(row_ptr, col_idx, vals_bits, bR, B_f32, br0=0, br1=None, threads=1):
+    """Block-sparse host multiply in fp32 (a CPU baseline, not a reference
+    algorithm): block rows [br0, br1) of A (BCSR, fp16 bits) times B (fp32)."""
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    ci = np.ascontiguousarray(col_idx, np.int32)
+    v = np.ascontiguousarray(vals_bits, np.uint16)
+    B = np.ascontiguousarray(B_f32, np.float32)
+    K, N = B.shape
+    br1 = len(rp) - 1 if br1 is None else br1
+    C = np.empty(((br1 - br0) * bR, N), np.float32)
+    lib().oracle_bcsr_matmul_f32_mt(_p(rp), _p(ci), _p(v), bR, _p(B), K, N, br0, br1, _p(C), int(threads))
     return C
 
 

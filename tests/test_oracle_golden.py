@@ -109,6 +109,20 @@ def test_fp64_bcsr_product_matches_dense():
     assert mx < 1e-6 and fr < 1e-6
 
 
+def test_block_sparse_host_baseline_exact():
+    """The block-sparse host multiply (the bench's all-core CPU baseline) on
+    integer-valued inputs, where every sum is exact in fp32, and its row split."""
+    rng = np.random.default_rng(2)
+    A = (rng.integers(-3, 4, (128, 96)) * (rng.random((128, 96)) < 0.2)).astype(np.float16)
+    hdr, idx, data = oracle.bcsr(A.view(np.uint16), 32, 16)
+    B = rng.integers(-3, 4, (96, 40)).astype(np.float32)
+    want = A.astype(np.float32) @ B
+    for threads in (1, 3):
+        C = oracle.bcsr_matmul_f32_mt(hdr, idx, data, 32, B, threads=threads)
+        assert np.array_equal(C, want)
+    assert np.array_equal(oracle.bcsr_matmul_f32_mt(hdr, idx, data, 32, B, 1, 3, threads=2), want[32:96])
+
+
 @pytest.mark.skipif(oracle.ref_lib() is None, reason="reference tree not built here")
 def test_oracle_against_live_reference_build():
     R = oracle.ref_lib()
