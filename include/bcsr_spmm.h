@@ -249,6 +249,15 @@ spmm_status spmm_hcsr_plan_destroy(spmm_hcsr_plan* plan);
 spmm_status spmm_csr_mm(const spmm_csr_desc* A, const spmm_dense_desc* B, int N, float* C, int ldc,
                         void* stream);
 
+/* Dense x dense (fp16 or bf16 A and B, fp32 C) on the tcgen05 tensor cores: the
+ * native dense comparator. It replaces the reference's denseMatrixMulTensor
+ * (src/cuda_kernels.cu:246-270, one WMMA warp per 16 x 16 tile) and its scalar
+ * dense kernels (src/cuda_kernels.cu:86-244). A is M x K row-major (lda >= K, a
+ * multiple of 8), B K x N row-major (ldb >= N, a multiple of 8), C M x N fp32
+ * (ldc >= N, a multiple of 4); N % 8 == 0; 16-byte aligned bases. Asynchronous. */
+spmm_status spmm_dense_mm(const void* A, int lda, const spmm_dense_desc* B, int M, int K, int N,
+                          spmm_dtype dtype, float* C, int ldc, void* stream);
+
 /* ---- tuning ----------------------------------------------------------------------
  * No counterpart in the reference (its harness sweeps kernels by hand).
  * The configuration space: a fixed table of spmm_tune_config_count() entries

@@ -40,6 +40,7 @@ from .bcsr import (  # noqa: F401
     hcsr_mm,
     HcsrPlan,
     csr_mm,
+    dense_mm,
     gpu_gen_structure,
     gpu_gen_values,
     gpu_gen_dense,

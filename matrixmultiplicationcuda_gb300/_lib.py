@@ -83,6 +83,8 @@ _SIGS = {
     "spmm_hcsr_plan_run": (c_int, [c_vp, ctypes.POINTER(DenseDesc), c_int, c_vp, c_int, ctypes.POINTER(Config),
                                    c_vp]),
     "spmm_hcsr_plan_destroy": (c_int, [c_vp]),
+    "spmm_dense_mm": (c_int, [c_vp, c_int, ctypes.POINTER(DenseDesc), c_int, c_int, c_int, c_int, c_vp, c_int,
+                              c_vp]),
     "spmm_hcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(CsrDesc), ctypes.POINTER(DenseDesc), c_int,
                              c_vp, c_int, ctypes.POINTER(Config), c_vp]),
     "sparseMatrixMulTensor_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),

@@ -169,6 +169,24 @@ class HcsrPlan:
             pass
 
 
+def dense_mm(A, B, C=None, stream=None):
+    """Dense A (M x K) @ B (K x N), fp16 or bf16 device tensors (row-major, rows
+    16-byte aligned), fp32 C, on the tcgen05 tensor cores: the native dense
+    comparator."""
+    torch = _torch()
+    M, K = int(A.shape[0]), int(A.shape[1])
+    N = int(B.shape[1])
+    if A.dtype != B.dtype or A.dtype not in (torch.float16, torch.bfloat16):
+        raise SpmmError(Status.UNSUPPORTED, "A and B must both be fp16 or both bf16")
+    dt = DType.BF16 if A.dtype == torch.bfloat16 else DType.F16
+    if C is None:
+        C = torch.empty((M, N), dtype=torch.float32, device=B.device)
+    b = _dense_desc(B, None, 1.0, ldb=B.stride(0))
+    check(lib().spmm_dense_mm(ctypes.c_void_p(A.data_ptr()), int(A.stride(0)), ctypes.byref(b), M, K, N, int(dt),
+                              ctypes.c_void_p(C.data_ptr()), int(C.stride(0)), stream_handle(stream)))
+    return C
+
+
 def csr_mm(row_ptr, col_idx, vals, K, B, N=None, C=None, stream=None, ldc=None):
     """CSR x dense (fp16, device tensors), C fp32: the native comparator."""
     from ._lib import CsrDesc
