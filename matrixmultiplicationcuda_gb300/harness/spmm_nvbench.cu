@@ -36,7 +36,8 @@
 //   launch  host time per call and back-to-back launch rate (L2 warm) on the
 //       c1 and c3 products (not part of "all").
 //   compare the same product as BCSR, CSR (native kernel), dense through the
-//       BCSR pipeline with every block stored, and cuBLAS GemmEx.
+//       BCSR pipeline with every block stored, the native dense GEMM, and
+//       cuBLAS GemmEx.
 //   hybrid  the hybrid BCSR + CSR product across density thresholds.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -570,8 +571,9 @@ class Runner {
   }
 
   // The same product as BCSR (cost-model configuration), as CSR (the native
-  // CSR kernel), and densely: the BCSR pipeline with every block stored, and
-  // cuBLAS GemmEx (fp16 in, fp32 out) as the library reference point.
+  // CSR kernel), and densely: the BCSR pipeline with every block stored, the
+  // native tcgen05 dense GEMM, and cuBLAS GemmEx (fp16 in, fp32 out) as the
+  // library reference point.
   void compare_bench(const Spec& spec, const char* label) {
     DeviceProduct P;
     build_product(spec, P);
@@ -650,6 +652,9 @@ class Runner {
     v.push_back({"CSR (native kernel)", timer_.measure([&] { SK(spmm_csr_mm(&R, &P.B, N, P.C, N, nullptr)); }, o_)});
     v.push_back({"dense: BCSR pipeline, all blocks, " + config_name(pcf),
                  timer_.measure([&] { SK(spmm_bcsr_mm(&F, &P.B, N, P.C, N, pcf, nullptr)); }, o_)});
+    v.push_back({"dense: native tcgen05 GEMM (spmm_dense_mm)", timer_.measure([&] {
+                   SK(spmm_dense_mm(d_dense, K, &P.B, M, K, N, SPMM_F16, P.C, N, nullptr));
+                 }, o_)});
     v.push_back({"dense: cuBLAS GemmEx (library)", timer_.measure([&] {
                    cublasGemmEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, M, K, &one, P.B.data, CUDA_R_16F, N, d_dense,
                                 CUDA_R_16F, K, &zero, P.C, CUDA_R_32F, N, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
