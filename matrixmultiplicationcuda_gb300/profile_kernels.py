@@ -20,6 +20,7 @@ Families (seeded synthetic inputs; a few hundred MB on the device at most):
   csr       k_csr_mm on the same matrix's entries, all as CSR
   tc64      k_bcsr_tc64 (64-row blocks, M=64 UMMAs, one CTA per SM): the tc
             product in fp16 and in split fp16, 256-column tile
+  dense     k_dense_tc: the native dense comparator, A 8192 x 8192, B 8192 x 1024, fp16
   gen       the GPU generators: k_gen_structure + k_gen_values for the tc
             product's structure (A 16384^2, 64x16, 2 %), k_gen_dense for B
             (16384 x 512), k_gen_matrix (reference blockrandom, 8192^2 fp16)
@@ -39,7 +40,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr,"
-                                      "tc64,gen")
+                                      "tc64,gen,dense")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args(argv)
     import torch
@@ -152,6 +153,13 @@ def main(argv=None):
         A, B, Blo, bs, C = c3(m.DType.F16_SPLIT)
         run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256), B_lo=Blo))
         print("tc64: nnzb=%d" % A.nnzb)
+    if "dense" in only:
+        g = torch.Generator().manual_seed(0)
+        Ad = (torch.rand((8192, 8192), generator=g) * 2 - 1).half().to(dev)
+        Bd = (torch.rand((8192, 1024), generator=g) * 2 - 1).half().to(dev)
+        Cd = torch.empty((8192, 1024), dtype=torch.float32, device=dev)
+        run(lambda: m.dense_mm(Ad, Bd, C=Cd))
+        print("dense: 8192 x 8192 x 1024")
     if "gen" in only:
         def gen():
             rp, ci = m.gpu_gen_structure(16384, 16384, 64, m.PATTERN_RANDOM, 0.02, 0, seed=20240, device=dev)
