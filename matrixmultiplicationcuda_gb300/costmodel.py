@@ -4,8 +4,8 @@ library's own CUDA kernels (spmm_mlp_forward / _backward / _adam).
 
 Training data are the autotuner's own sweeps on seeded synthetic products
 (collect()); the trained network replaces the sweep at launch
-(CostModel.select), and the sweep stays the fallback and the judge of its
-regret (evaluate()).
+(CostModel.select), and the sweep stays the fallback and the yardstick for
+its regret (evaluate()).
 """
 import ctypes
 import math
