@@ -27,7 +27,7 @@ extern "C" {
 typedef enum spmm_status {
   SPMM_OK = 0,
   SPMM_ERR_INVALID_ARG = 1,    /* null pointer, negative size, bad block shape   */
-  SPMM_ERR_UNSUPPORTED = 2,    /* a shape or dtype this build has no kernel for  */
+  SPMM_ERR_UNSUPPORTED = 2,    /* a shape or dtype the library has no kernel for */
   SPMM_ERR_MISALIGNED = 3,     /* a pointer or leading dimension breaks TMA rules */
   SPMM_ERR_CUDA = 4,           /* a CUDA runtime / driver call failed             */
   SPMM_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up              */
