@@ -370,8 +370,18 @@ def run_ours(args, world, rank, local):
         return out
 
     def launch(prob, cfg, stream=None):
+        """One product on a configuration, or on a per-matrix plan (m.BcsrPlan)."""
         A, Bq, Blo, bs, C = prob
-        m.spmm(A, Bq, N=N, C=C, cfg=cfg, B_lo=Blo, b_scale=bs, stream=stream)
+        if isinstance(cfg, m.BcsrPlan):
+            cfg.run(A, Bq, C=C, B_lo=Blo, b_scale=bs, stream=stream)
+        else:
+            m.spmm(A, Bq, N=N, C=C, cfg=cfg, B_lo=Blo, b_scale=bs, stream=stream)
+
+    def cfg_name(c):
+        if isinstance(c, m.BcsrPlan):
+            items, groups, pc = c.info()
+            return "plan %s (%d rows split)" % (tuner.config_name(pc), groups)
+        return tuner.config_name(c)
 
     stream = torch.cuda.current_stream()
 
@@ -402,14 +412,29 @@ def run_ours(args, world, rank, local):
         ms_sweep = tuner.sweep(A0, Bq0, N, C0, warmup=2, reps=5, flush=flush, B_lo=Blo0)
         cfg_model = model.select(A0, N)
         cfg_sweep = table[int(np.argmin(ms_sweep))]
+        # the model's pick on the tcgen05 pipeline also runs on a per-matrix plan
+        # (heaviest-first items, rows far above the average load split)
+        plan = None
+        if cfg_model.kernel == 2 and cfg_model.split_k <= 1 and cfg_model.schedule == 0:
+            try:
+                plan = m.BcsrPlan(A0, N, cfg_model)
+            except m.SpmmError:
+                plan = None
         time_loop(probs, cfg_model, 3)
         time_loop(probs, cfg_sweep, 3)
         t_model = time_loop(probs, cfg_model, 30)
         t_sweep = time_loop(probs, cfg_sweep, 30)
+        t_plan = None
+        if plan is not None:
+            time_loop(probs, plan, 3)
+            t_plan = time_loop(probs, plan, 30)
         m.device_error_check()
-        sys.stderr.write("%s: model pick %s %.2f us, sweep best %s %.2f us\n" % (
-            name, tuner.config_name(cfg_model), t_model * 1e3, tuner.config_name(cfg_sweep), t_sweep * 1e3))
-        results[name] = {"ms": t_model, "cfg": cfg_model, "tflops": flops / t_model / 1e9,
+        best_cfg, best_ms = (plan, t_plan) if t_plan is not None and t_plan < t_model else (cfg_model, t_model)
+        sys.stderr.write("%s: model pick %s %.2f us (on a plan: %s), sweep best %s %.2f us\n" % (
+            name, tuner.config_name(cfg_model), t_model * 1e3,
+            "%.2f us" % (t_plan * 1e3) if t_plan is not None else "n/a", tuner.config_name(cfg_sweep), t_sweep * 1e3))
+        results[name] = {"ms": best_ms, "cfg": best_cfg, "model_cfg": cfg_model, "model_ms": t_model,
+                         "plan_ms": t_plan, "tflops": flops / best_ms / 1e9,
                          "sweep_ms": t_sweep, "sweep_cfg": cfg_sweep,
                          "err_bar": ERROR_BAR[name], "bytes": algorithmic_bytes(nnzb, cols_touched, name)}
     model.close()
@@ -485,13 +510,18 @@ def run_ours(args, world, rank, local):
                     dx[-1] if A0.scales is not None else None)
         sets.append((dA + dx + dB, Ae, dB, torch.empty((M, N), dtype=torch.float32, device=dev)))
 
+    # a plan with split rows runs one launch at a time: one per stream
+    e2e_cfgs = [cfg, cfg]
+    if isinstance(cfg, m.BcsrPlan) and cfg.info()[1] > 0:
+        e2e_cfgs[1] = m.BcsrPlan(A0, N, cfg.info()[2])
+
     def e2e_step(i):
         dev_bufs, Ae, dB, Cd = sets[i % 2]
         st = streams[i % 2]
         with torch.cuda.stream(st):
             for d, h in zip(dev_bufs, hA + hx + hB):
                 d.copy_(h, non_blocking=True)
-            m.spmm(Ae, dB[0], N=N, C=Cd, cfg=cfg, B_lo=dB[1] if len(dB) > 1 else None, b_scale=bs0, stream=st)
+            launch((Ae, dB[0], dB[1] if len(dB) > 1 else None, bs0, Cd), e2e_cfgs[i % 2], stream=st)
             hC[i % 2].copy_(Cd, non_blocking=True)
 
     e2e_steps = max(4, min(args.steps, 50))
@@ -557,7 +587,7 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": tuned, "data": "synthetic (seeded generators)",
             "config": {"workload": WORKLOAD, "precision": tuned,
-                       "kernel_config": tuner.config_name(cfg), "picked_by": "learned cost model",
+                       "kernel_config": cfg_name(cfg), "picked_by": "learned cost model",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
                        "nnzb": nnzb},
@@ -565,7 +595,8 @@ def run_ours(args, world, rank, local):
                            "kernel_config": "library default (no tuning)"},
             "tuned_vs_plain_fp16": plain_ms / tr["ms"],
             "precisions": {k: {"tflops": v["tflops"], "ms": v["ms"], "err_bar": v["err_bar"],
-                               "model_pick": tuner.config_name(v["cfg"]),
+                               "model_pick": tuner.config_name(v["model_cfg"]), "run_as": cfg_name(v["cfg"]),
+                               "model_pick_ms": v["model_ms"], "on_plan_ms": v["plan_ms"],
                                "sweep_best": tuner.config_name(v["sweep_cfg"]), "sweep_best_ms": v["sweep_ms"],
                                "model_regret": v["ms"] / v["sweep_ms"] - 1.0,
                                "max_rel_err": v["max_rel"], "fro_rel_err": v["fro_rel"]}

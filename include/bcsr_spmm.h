@@ -331,6 +331,27 @@ spmm_status spmm_cost_model_destroy(spmm_cost_model* model);
 spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr_desc* A, int N,
                                    spmm_config* out, float* predicted_ms, void* stream);
 
+/* ---- per-matrix plan (tcgen05 pipeline) ----------------------------------------
+ * A launch is bound by its longest CTA, and one block row (and column tile) is
+ * one CTA's item. _create reads row_ptr once (it synchronises `stream`) and
+ * builds an item list ordered heaviest first. A row longer than 3x the
+ * average load per CTA slot is cut into parts of about that load, run by
+ * different CTAs: part 0 zeroes the row's C tile while its MMAs run, and
+ * every part adds its tile into C with red.add (so C of those rows is summed
+ * in an order that varies from run to run within fp32 rounding). _run is one
+ * launch; A must have the plan's M, K, block shape, dtype and row_ptr (column
+ * indices and values may differ), and N must be the plan's. One plan runs
+ * one launch at a time. cfg: kernel 0 or 2, no split-K, static schedule.
+ * spmm_bcsr_plan_info: item count, split rows (row and column-tile pairs),
+ * and the configuration the plan runs. */
+typedef struct spmm_bcsr_plan spmm_bcsr_plan;
+spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, const spmm_config* cfg, void* stream,
+                                  spmm_bcsr_plan** plan_out);
+spmm_status spmm_bcsr_plan_info(const spmm_bcsr_plan* plan, int* items, int* split_rows, spmm_config* cfg);
+spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* plan, const spmm_bcsr_desc* A, const spmm_dense_desc* B,
+                               int N, float* C, int ldc, void* stream);
+spmm_status spmm_bcsr_plan_destroy(spmm_bcsr_plan* plan);
+
 /* ---- allocation-free variant ---------------------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc (a
  * host application or allocator that owns all device memory, a memory budget

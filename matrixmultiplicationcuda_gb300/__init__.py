@@ -39,6 +39,7 @@ from .bcsr import (  # noqa: F401
     BatchPlan,
     hcsr_mm,
     HcsrPlan,
+    BcsrPlan,
     csr_mm,
     dense_mm,
     gpu_gen_structure,

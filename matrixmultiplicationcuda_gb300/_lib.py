@@ -83,6 +83,12 @@ _SIGS = {
     "spmm_hcsr_plan_run": (c_int, [c_vp, ctypes.POINTER(DenseDesc), c_int, c_vp, c_int, ctypes.POINTER(Config),
                                    c_vp]),
     "spmm_hcsr_plan_destroy": (c_int, [c_vp]),
+    "spmm_bcsr_plan_create": (c_int, [ctypes.POINTER(BcsrDesc), c_int, ctypes.POINTER(Config), c_vp,
+                                      ctypes.POINTER(c_vp)]),
+    "spmm_bcsr_plan_info": (c_int, [c_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(Config)]),
+    "spmm_bcsr_plan_run": (c_int, [c_vp, ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp, c_int,
+                                   c_vp]),
+    "spmm_bcsr_plan_destroy": (c_int, [c_vp]),
     "spmm_dense_mm": (c_int, [c_vp, c_int, ctypes.POINTER(DenseDesc), c_int, c_int, c_int, c_int, c_vp, c_int,
                               c_vp]),
     "spmm_hcsr_mm": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(CsrDesc), ctypes.POINTER(DenseDesc), c_int,

@@ -122,6 +122,49 @@ def hcsr_mm(A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, B, N=None, C=Non
     return C
 
 
+class BcsrPlan:
+    """A per-matrix plan for the tcgen05 pipeline (spmm_bcsr_plan_*): the item
+    list ordered heaviest first, with the longest block rows split across the
+    CTA slots the rows leave spare. Built once from A's row_ptr; run() is one
+    launch on any A with the same structure."""
+
+    def __init__(self, A: BCSR, N, cfg: Optional[Config] = None, stream=None):
+        a = A.desc()
+        h = ctypes.c_void_p()
+        check(lib().spmm_bcsr_plan_create(ctypes.byref(a), int(N), ctypes.byref(cfg) if cfg is not None else None,
+                                          stream_handle(stream), ctypes.byref(h)))
+        self._h = h
+        self.M, self.N = A.M, int(N)
+
+    def info(self):
+        """(items, split rows, the configuration it runs)."""
+        n, sp, c = ctypes.c_int(), ctypes.c_int(), Config()
+        check(lib().spmm_bcsr_plan_info(self._h, ctypes.byref(n), ctypes.byref(sp), ctypes.byref(c)))
+        return n.value, sp.value, c
+
+    def run(self, A: BCSR, B, C=None, stream=None, B_lo=None, b_scale=1.0, ldc=None):
+        torch = _torch()
+        if C is None:
+            C = torch.empty((self.M, self.N), dtype=torch.float32, device=B.device)
+        ldc = int(C.stride(0)) if ldc is None else int(ldc)
+        a = A.desc()
+        b = _dense_desc(B, B_lo, b_scale, ldb=B.stride(0))
+        check(lib().spmm_bcsr_plan_run(self._h, ctypes.byref(a), ctypes.byref(b), self.N,
+                                       ctypes.c_void_p(C.data_ptr()), ldc, stream_handle(stream)))
+        return C
+
+    def close(self):
+        if self._h:
+            lib().spmm_bcsr_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class HcsrPlan:
     """The planned hybrid product (fp16, 16x16 blocks): the CSR part packed once
     into gather blocks that the tcgen05 pipeline runs beside the stored blocks.

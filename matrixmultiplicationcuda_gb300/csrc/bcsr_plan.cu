@@ -1,0 +1,189 @@
+// A per-matrix plan for the tcgen05 pipeline: an item list ordered heaviest
+// first, with block rows far longer than the rest split into parts.
+//
+// A launch of k_bcsr_tc is bound by its longest CTA: one item is a block row
+// (and column tile), and a CTA streams its blocks at a fixed rate, so a row
+// many times longer than the average sets the time while other CTAs idle. The
+// plan reads row_ptr once. A row longer than 3x the average load per CTA slot
+// is cut into parts of about that load, run by different CTAs: part 0 zeroes
+// the row's C tile while its MMAs run, and every part adds its tile into C
+// with red.add once that is done. Rows not split store C directly, as without
+// a plan; on rows of similar lengths (no row that long) the plan only orders
+// the items.
+//
+// The plan holds only what row_ptr determines: any A with the same M, K, block
+// shape, dtype and row_ptr (values and column indices may change) runs on it.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+#include "internal.h"
+
+struct spmm_bcsr_plan {
+  int M = 0, K = 0, bR = 0, N = 0;
+  spmm_dtype dtype = SPMM_F16;
+  spmm_config cfg{};
+  int n_items = 0, n_pairs = 0;
+  int4* items = nullptr;       // {block row, column tile, first block, end block}
+  int* pair = nullptr;         // -1, or 128 * group + part
+  int* parts = nullptr;        // parts per group (split row and tile)
+  unsigned* counters = nullptr;   // per group: {C tile zeroed, parts finished}
+};
+
+namespace spmm {
+namespace {
+
+constexpr int kMinPartBlocks = 8;   // shorter parts are not worth a hand-off
+constexpr int kSplitFactor = 3;     // split rows longer than 3x the average load per CTA slot
+constexpr int kMaxParts = 64;
+
+void plan_free(spmm_bcsr_plan* p) {
+  if (!p) return;
+  cudaFree(p->items);
+  cudaFree(p->pair);
+  cudaFree(p->parts);
+  cudaFree(p->counters);
+  delete p;
+}
+
+}  // namespace
+}  // namespace spmm
+
+using namespace spmm;
+
+extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, const spmm_config* cfg, void* stream,
+                                             spmm_bcsr_plan** out) {
+  if (!out) return fail(SPMM_ERR_INVALID_ARG, "null output");
+  *out = nullptr;
+  if (!A) return fail(SPMM_ERR_INVALID_ARG, "null descriptor");
+  if (A->M <= 0 || A->K <= 0 || N <= 0) return fail(SPMM_ERR_INVALID_ARG, "a plan needs a non-empty product");
+  if (A->bC != 16 || (A->bR != 16 && A->bR != 32 && A->bR != 64))
+    return fail(SPMM_ERR_UNSUPPORTED, "block shape must be 16, 32 or 64 x 16");
+  if (A->M % A->bR || A->K % 16) return fail(SPMM_ERR_INVALID_ARG, "M / K not multiples of the block shape");
+  if (N % 8) return fail(SPMM_ERR_UNSUPPORTED, "N must be a multiple of 8");
+  if (!A->row_ptr) return fail(SPMM_ERR_INVALID_ARG, "null row_ptr");
+  spmm_config c;
+  std::memset(&c, 0, sizeof(c));
+  if (cfg) c = *cfg;
+  if (c.kernel != 0 && c.kernel != 2) return fail(SPMM_ERR_UNSUPPORTED, "a plan runs on kernel 2");
+  if (c.split_k > 1 || c.schedule != 0)
+    return fail(SPMM_ERR_UNSUPPORTED, "a plan replaces split-K and the work queue");
+  c.kernel = 2;
+  int nt = 0, per_sm = 0;
+  if (!tc_geometry(A->bR, A->dtype, N, c, &nt, &per_sm))
+    return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for this block height, dtype and configuration");
+  c.n_tile = nt;
+  const int MB = A->M / A->bR;
+  std::vector<int> rp(MB + 1);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  SPMM_CUDA_TRY(cudaMemcpyAsync(rp.data(), A->row_ptr, sizeof(int) * (MB + 1), cudaMemcpyDeviceToHost, s));
+  SPMM_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int r = 0; r < MB; ++r)
+    if (rp[r + 1] < rp[r]) return fail(SPMM_ERR_INVALID_ARG, "row_ptr must not decrease");
+  const int ntiles = (N + nt - 1) / nt;
+  const long long base = (long long)MB * ntiles;
+  const long long capacity = (long long)sm_count() * per_sm;
+  // the average load per CTA slot, and the rows far above it
+  long long total = 0;
+  for (int r = 0; r < MB; ++r) total += (long long)(rp[r + 1] - rp[r]) * ntiles;
+  const long long avg = std::max<long long>(kMinPartBlocks, (total + capacity - 1) / capacity);
+  struct Item {
+    int4 d;
+    int pair;
+  };
+  std::vector<Item> items;
+  std::vector<int> group_parts;
+  items.reserve((size_t)base + 64);
+  for (int r = 0; r < MB; ++r) {
+    const int len = rp[r + 1] - rp[r];
+    const int k = len > kSplitFactor * avg ? (int)std::min<long long>(kMaxParts, (len + avg - 1) / avg) : 1;
+    for (int t = 0; t < ntiles; ++t) {
+      if (k == 1) {
+        items.push_back({make_int4(r, t, rp[r], rp[r + 1]), -1});
+        continue;
+      }
+      const int g = (int)group_parts.size();
+      group_parts.push_back(k);
+      for (int q = 0; q < k; ++q)
+        items.push_back({make_int4(r, t, rp[r] + (int)((long long)len * q / k), rp[r] + (int)((long long)len * (q + 1) / k)),
+                         128 * g + q});
+    }
+  }
+  const int pairs = (int)group_parts.size();
+  if (items.size() >= (1u << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
+  // heaviest first: with more items than CTAs, each CTA's next item is lighter
+  std::stable_sort(items.begin(), items.end(),
+                   [](const Item& a, const Item& b) { return a.d.w - a.d.z > b.d.w - b.d.z; });
+  std::vector<int4> hd(items.size());
+  std::vector<int> hp(items.size());
+  for (size_t i = 0; i < items.size(); ++i) {
+    hd[i] = items[i].d;
+    hp[i] = items[i].pair;
+  }
+  spmm_bcsr_plan* p = new spmm_bcsr_plan;
+  p->M = A->M;
+  p->K = A->K;
+  p->bR = A->bR;
+  p->N = N;
+  p->dtype = A->dtype;
+  p->cfg = c;
+  p->n_items = (int)items.size();
+  p->n_pairs = pairs;
+  if (cudaMalloc(&p->items, sizeof(int4) * hd.size()) != cudaSuccess ||
+      cudaMalloc(&p->pair, sizeof(int) * hp.size()) != cudaSuccess ||
+      cudaMalloc(&p->parts, sizeof(int) * std::max(pairs, 1)) != cudaSuccess ||
+      cudaMalloc(&p->counters, sizeof(unsigned) * 2 * std::max(pairs, 1)) != cudaSuccess) {
+    plan_free(p);
+    return fail(SPMM_ERR_CUDA, "plan allocation failed");
+  }
+  if (cudaMemcpy(p->items, hd.data(), sizeof(int4) * hd.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->pair, hp.data(), sizeof(int) * hp.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      (pairs > 0 && cudaMemcpy(p->parts, group_parts.data(), sizeof(int) * pairs, cudaMemcpyHostToDevice) != cudaSuccess) ||
+      cudaMemset(p->counters, 0, sizeof(unsigned) * 2 * std::max(pairs, 1)) != cudaSuccess) {
+    plan_free(p);
+    return fail(SPMM_ERR_CUDA, "plan upload failed");
+  }
+  *out = p;
+  return SPMM_OK;
+}
+
+extern "C" spmm_status spmm_bcsr_plan_info(const spmm_bcsr_plan* p, int* items, int* split_rows, spmm_config* cfg) {
+  if (!p) return fail(SPMM_ERR_INVALID_ARG, "null plan");
+  if (items) *items = p->n_items;
+  if (split_rows) *split_rows = p->n_pairs;
+  if (cfg) *cfg = p->cfg;
+  return SPMM_OK;
+}
+
+extern "C" spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* p, const spmm_bcsr_desc* A, const spmm_dense_desc* B,
+                                          int N, float* C, int ldc, void* stream) {
+  if (!p || !A || !B) return fail(SPMM_ERR_INVALID_ARG, "null plan or descriptor");
+  if (A->M != p->M || A->K != p->K || A->bR != p->bR || A->dtype != p->dtype || N != p->N)
+    return fail(SPMM_ERR_INVALID_ARG, "A and N must match the plan");
+  if (!A->row_ptr || !C || !B->data) return fail(SPMM_ERR_INVALID_ARG, "null pointer");
+  if (B->ldb < N || B->ldb % 8) return fail(SPMM_ERR_MISALIGNED, "ldb must be >= N and a multiple of 8");
+  if (ldc < N || ldc % 4) return fail(SPMM_ERR_MISALIGNED, "ldc must be >= N and a multiple of 4");
+  auto al16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  if ((A->vals && !al16(A->vals)) || !al16(B->data) || !al16(C))
+    return fail(SPMM_ERR_MISALIGNED, "A values, B and C must be 16-byte aligned");
+  LaunchRequest r;
+  r.A = A;
+  r.B = B;
+  r.N = N;
+  r.C = C;
+  r.ldc = ldc;
+  r.cfg = p->cfg;
+  r.stream = static_cast<cudaStream_t>(stream);
+  r.items = p->items;
+  r.pair = p->n_pairs > 0 ? p->pair : nullptr;
+  r.parts = p->parts;
+  r.counters = p->counters;
+  r.plan_items = p->n_items;
+  return launch_tc(r);
+}
+
+extern "C" spmm_status spmm_bcsr_plan_destroy(spmm_bcsr_plan* p) {
+  plan_free(p);
+  return SPMM_OK;
+}

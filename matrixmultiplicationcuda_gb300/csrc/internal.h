@@ -81,7 +81,17 @@ struct LaunchRequest {
   // stored and gather blocks
   const int* gather_rows = nullptr;
   long long total_blocks = 0;
+  // planned product (kernel 2): the item list, split-row pairs and their
+  // counters (see spmm_bcsr_plan_create)
+  const int4* items = nullptr;
+  const int* pair = nullptr;
+  const int* parts = nullptr;
+  unsigned* counters = nullptr;
+  int plan_items = 0;
 };
+// The tcgen05 pipeline's column tile and CTAs per SM for a product (false when
+// it has no kernel for it): what a plan builds its item list for.
+bool tc_geometry(int bR, spmm_dtype dtype, int N, const spmm_config& cfg, int* nt, int* ctas_per_sm);
 // mma.sync family (spmm_mma.cu)
 spmm_status launch_mma(const LaunchRequest& r);
 // tcgen05 family (spmm_tc.cu); returns SPMM_ERR_UNSUPPORTED when it has no kernel for r

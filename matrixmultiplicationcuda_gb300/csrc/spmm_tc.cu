@@ -65,7 +65,27 @@ struct TcParams {
   // planned hybrid product: a block with col_idx = -(g + 1) is a gather block,
   // whose panel rows are B rows gather_rows[16g .. 16g + 15] (NULL: none)
   const int* gather_rows;
+  // planned product (items NULL: item v is block row v / (ntiles * split)):
+  // item v = items[v] = {block row, column tile, first block, end block}.
+  // pair[v] = -1, or 128 * g + q for part q of split row (and tile) g, which
+  // has parts[g] parts. Part 0 zeroes the C tile as soon as it takes the item
+  // (its MMAs still running) and sets counters[2g]; every part waits for that
+  // flag (bounded) and adds its tile into C with red.add; the last part to
+  // count itself in counters[2g + 1] sets both back to zero.
+  const int4* items;
+  const int* pair;
+  const int* parts;
+  unsigned* counters;
 };
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* ptr) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* ptr, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(ptr), "r"(v) : "memory");
+}
 
 // BR: block height (the UMMA N); NT: output columns per item; STAGES: ring
 // depth in groups; ACC: TMEM accumulators per CTA (2 = one item's epilogue
@@ -122,6 +142,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const uint32_t qfull0 = done_bar + 8, qempty0 = qfull0 + 8 * kQ;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5 + 2 * kQ);
   int* s_item = reinterpret_cast<int*>(tmem_slot + 1);      // kQ x {item, start, end}
+  int* s_role = s_item + 3 * kQ;                            // a split row's role, set by the epilogue
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 32) {
@@ -191,6 +212,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       auto range = [&](int v, int* s0, int* s1) {
         if (v < 0) {
           *s0 = *s1 = 0;
+          return;
+        }
+        if (p.items) {
+          const int4 d = __ldg(p.items + v);
+          *s0 = d.z;
+          *s1 = d.w;
           return;
         }
         const int row = v / (p.ntiles * p.split);
@@ -280,7 +307,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       start = __shfl_sync(0xffffffffu, start, 0);
       end = __shfl_sync(0xffffffffu, end, 0);
       if (!ok || item < 0) break;
-      const int nt = (item / p.split) % p.ntiles;
+      const int nt = p.items ? __ldg(&p.items[item].y) : (item / p.split) % p.ntiles;
       int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
@@ -406,6 +433,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     // ------------------------------ epilogue (warps 4-7) ---------------------------
     const int q4 = warp & 3;                // TMEM lane quarter this warp may access
     const bool hybrid = p.csr_row_ptr != nullptr;
+    const bool planned = p.pair != nullptr;
     for (uint32_t it = 0;; ++it) {
       int item = -1, start = 0, end = 0, ok = 1;
       if (lane == 0) ok = read_item(it, &item, &start, &end, 16u) ? 1 : 0;
@@ -413,45 +441,108 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       item = __shfl_sync(0xffffffffu, item, 0);
       const bool empty = __shfl_sync(0xffffffffu, start == end ? 1 : 0, 0) != 0;
       bool leave = !ok || item < 0;
+      int br = 0, nt = 0, grp = -1, part = 0;
+      if (!leave) {
+        if (p.items) {
+          const int4 d = __ldg(p.items + item);
+          br = d.x;
+          nt = d.y;
+        } else {
+          br = item / (p.ntiles * p.split);
+          nt = (item / p.split) % p.ntiles;
+        }
+        if (planned) {
+          const int code = __ldg(p.pair + item);
+          if (code >= 0) {
+            grp = code >> 7;
+            part = code & 127;
+          }
+        }
+      }
+      const long long row0 = (long long)br * BR;
+      // The hybrid pass and the split-row protocol synchronise the four
+      // epilogue warps, so they agree on leaving (a reduction over the same
+      // named barrier) and no warp is left waiting for one that has gone.
+      if (planned) {
+        if (bar_red_or(1, 128, leave)) break;
+        if (grp >= 0 && part == 0) {
+          // part 0 of a split row: zero its C tile while the MMAs run
+          const int n0 = nt * NT, n1 = min(nt * NT + NT, p.N);
+          for (int r = q4; r < BR; r += 4) {
+            float* crow = p.C + (row0 + r) * p.ldc;
+            for (int n = n0 + lane * 4; n < n1; n += 128) __stcg(reinterpret_cast<float4*>(crow + n), make_float4(0.f, 0.f, 0.f, 0.f));
+          }
+          __threadfence();
+          bar_sync_named(1, 128);
+          if (warp == 4 && lane == 0) st_release_gpu(p.counters + 2 * grp, 1u);
+        }
+      }
       if (!leave && !mbar_wait(tfull0 + 8 * (it % ACC), (it / ACC) & 1, p.timeout_ns)) {
         if (lane == 0) atomicOr(p.err, 16u);
         leave = true;
       }
-      // The hybrid pass below synchronises the four epilogue warps, so they
-      // agree on leaving (a reduction over the same named barrier) and no warp
-      // is left waiting for one that has gone.
-      if (hybrid ? bar_red_or(1, 128, leave) : leave) break;
+      if ((hybrid || planned) ? bar_red_or(1, 128, leave) : leave) break;
       tc_fence_after();
       const uint32_t acc = (it % ACC);
-      const int br = item / (p.ntiles * p.split), nt = (item / p.split) % p.ntiles;
-      const long long row0 = (long long)br * BR;
-#pragma unroll 1
-      for (int j = 0; j < Cfg::kJ; ++j) {
-        const int n = nt * NT + j * 128 + q4 * 32 + lane;
-        float* cptr = p.C + row0 * p.ldc + n;
-        const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + acc * Cfg::kAccCols + j * BR;
-#pragma unroll
-        for (int c0 = 0; c0 < BR; c0 += 16) {
-          float v[16];
-          if (!empty) {
-            tmem_ld16(taddr + c0, v);
-          } else {
-#pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = 0.f;
+      // a part of a split row adds into C once part 0 has zeroed it (role 2);
+      // role 3: the wait gave up (error word set), nothing is added
+      int role = 0;
+      if (grp >= 0) {
+        if (warp == 4 && lane == 0) {
+          int r = 2;
+          const uint64_t t0 = global_timer_ns();
+          while (ld_acquire_gpu(p.counters + 2 * grp) == 0) {
+            if (global_timer_ns() - t0 > p.timeout_ns) {
+              atomicOr(p.err, 32u);
+              r = 3;
+              break;
+            }
+            __nanosleep(64);
           }
-          if (n < p.N) {
-            if (hybrid) {
-              // read back by the CSR pass below: keep the lines in L2
+          *s_role = r;
+        }
+        bar_sync_named(1, 128);
+        role = *reinterpret_cast<volatile int*>(s_role);
+        __threadfence();
+      }
+      if (role != 3) {
+#pragma unroll 1
+        for (int j = 0; j < Cfg::kJ; ++j) {
+          const int n = nt * NT + j * 128 + q4 * 32 + lane;
+          float* cptr = p.C + row0 * p.ldc + n;
+          const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + acc * Cfg::kAccCols + j * BR;
 #pragma unroll
-              for (int i = 0; i < 16; ++i) cptr[(long long)(c0 + i) * p.ldc] = v[i];
-            } else if (p.split == 1) {
+          for (int c0 = 0; c0 < BR; c0 += 16) {
+            float v[16];
+            if (!empty) {
+              tmem_ld16(taddr + c0, v);
+            } else {
 #pragma unroll
-              for (int i = 0; i < 16; ++i) __stcs(cptr + (long long)(c0 + i) * p.ldc, v[i]);
-            } else if (!empty) {
+              for (int i = 0; i < 16; ++i) v[i] = 0.f;
+            }
+            if (n < p.N) {
+              if (hybrid) {
+                // read back by the CSR pass below: keep the lines in L2
 #pragma unroll
-              for (int i = 0; i < 16; ++i) atomicAdd(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+                for (int i = 0; i < 16; ++i) cptr[(long long)(c0 + i) * p.ldc] = v[i];
+              } else if (role == 2 || (p.split > 1 && !empty)) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) atomicAdd(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+              } else if (p.split == 1) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) __stcs(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+              }
             }
           }
+        }
+      }
+      if (grp >= 0) {
+        // count this part in; the last one resets the pair's counters
+        __threadfence();
+        bar_sync_named(1, 128);
+        if (warp == 4 && lane == 0 && atomicAdd(p.counters + 2 * grp + 1, 1u) == (unsigned)__ldg(p.parts + grp) - 1u) {
+          p.counters[2 * grp] = 0u;
+          p.counters[2 * grp + 1] = 0u;
         }
       }
       tc_fence_before();
@@ -539,6 +630,19 @@ bool tc_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg) {
          (cfg.n_tile <= 0 || nt == cfg.n_tile);
 }
 
+bool tc_geometry(int bR, spmm_dtype dtype, int N, const spmm_config& cfg, int* nt, int* ctas_per_sm) {
+  const int mode = tc_mode(dtype);
+  if (mode < 0) return false;
+  const TcEntry* e = find_tc(bR, mode, N, cfg, nt);
+  if (!e) return false;
+  const int tmem_fit = 512 / e->tmem_cols;
+  const int smem_fit = smem_per_sm() / (int)(e->smem + 1024);
+  int per_sm = std::min(2, std::min(tmem_fit, smem_fit));
+  if (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < per_sm) per_sm = cfg.ctas_per_sm;
+  *ctas_per_sm = per_sm < 1 ? 1 : per_sm;
+  return true;
+}
+
 spmm_status launch_tc(const LaunchRequest& r) {
   const spmm_bcsr_desc& A = *r.A;
   const spmm_dense_desc& B = *r.B;
@@ -623,6 +727,15 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.Bh = static_cast<const __half*>(B.data);
   p.ldb = B.ldb;
   p.gather_rows = r.gather_rows;
+  p.items = r.items;
+  p.pair = r.pair;
+  p.parts = r.parts;
+  p.counters = r.counters;
+  if (r.items) {
+    if (p.split > 1 || r.csr || r.gather_rows || p.queue)
+      return fail(SPMM_ERR_UNSUPPORTED, "a planned product runs without split-K, CSR part or work queue");
+    p.n_items = r.plan_items;
+  }
   if (r.csr && (p.split > 1 || mode != MODE_F16))
     return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product runs in fp16 without split-K");
   if (!p.err) return fail(SPMM_ERR_CUDA, "could not set up the device error word");

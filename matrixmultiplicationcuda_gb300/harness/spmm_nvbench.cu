@@ -14,7 +14,7 @@
 // algorithmic GB/s, and the fraction of the roofline
 //   t_roof = max(FLOPs / tensor peak, compulsory bytes / HBM peak).
 //
-//   spmm_nvbench [--preset c1|c2|c3|c4|launch|compare|hybrid|all] [--tuning default,model,sweep]
+//   spmm_nvbench [--preset c1|c2|c3|c4|launch|compare|hybrid|all] [--tuning default,model,plan,sweep]
 //                [--min-samples 20] [--min-time 0.2] [--max-time 2]
 //                [--csv FILE] [--json FILE] [--model FILE] [--peaks FILE]
 //                [--filter SUBSTRING] [--no-check]
@@ -448,8 +448,30 @@ class Runner {
       Row r;
       r.spec = spec;
       r.tuning = tuning;
-      r.config = config_name(pc);
-      r.s = timer_.measure([&] { SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, pc, nullptr)); }, o_);
+      if (tuning == "plan") {
+        // the per-matrix plan on the tcgen05 pipeline: the model's configuration
+        // when it runs there (without split-K or the work queue), else its default
+        spmm_config mc{};
+        if (model_) SK(spmm_cost_model_select(model_, &P.A, P.N, &mc, nullptr, nullptr));
+        if (mc.kernel == 2) {
+          mc.split_k = 0;
+          mc.schedule = 0;
+        } else {
+          std::memset(&mc, 0, sizeof(mc));
+          mc.kernel = 2;
+        }
+        spmm_bcsr_plan* plan = nullptr;
+        if (spmm_bcsr_plan_create(&P.A, P.N, &mc, nullptr, &plan) != SPMM_OK) continue;   // no tcgen05 kernel
+        int items = 0, groups = 0;
+        spmm_config pcfg{};
+        SK(spmm_bcsr_plan_info(plan, &items, &groups, &pcfg));
+        r.config = "plan " + config_name(&pcfg) + " (" + std::to_string(groups) + " rows split)";
+        r.s = timer_.measure([&] { SK(spmm_bcsr_plan_run(plan, &P.A, &P.B, P.N, P.C, P.N, nullptr)); }, o_);
+        SK(spmm_bcsr_plan_destroy(plan));
+      } else {
+        r.config = config_name(pc);
+        r.s = timer_.measure([&] { SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, pc, nullptr)); }, o_);
+      }
       SK(spmm_device_error_check(nullptr));
       r.rel_err = o_.check ? check_rows(P, 2) : NAN;
       finish_row(r, P, pk_);
@@ -853,7 +875,7 @@ int main(int argc, char** argv) {
     } else if (a == "--no-check") {
       o.check = false;
     } else {
-      std::fprintf(stderr, "usage: spmm_nvbench [--preset c1,c2,c3,c4|all] [--tuning default,model,sweep] "
+      std::fprintf(stderr, "usage: spmm_nvbench [--preset c1,c2,c3,c4|all] [--tuning default,model,plan,sweep] "
                            "[--min-samples N] [--min-time S] [--max-time S] [--csv F] [--json F] [--model F] "
                            "[--peaks F] [--filter S] [--no-check]\n");
       return a == "--help" || a == "-h" ? 0 : 1;

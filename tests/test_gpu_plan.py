@@ -1,0 +1,106 @@
+"""The per-matrix plan (spmm_bcsr_plan_*): heaviest-first items, with rows far
+longer than the average load per CTA split into parts that add into a C tile
+their part 0 zeroed. Checked exactly at the headline size with integer inputs
+(row / column checksums, three runs in a row so the counters reset), against
+the unplanned product and FP64 with random values, with and without split
+rows, at ragged N, for every block height, and the argument checks."""
+import numpy as np
+import pytest
+
+import matrixmultiplicationcuda_gb300 as m
+from oracle import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("pattern,param,cfg", [
+    (m.PATTERN_RANDOM, 0.0, m.Config(kernel=2, n_tile=512, acc_buffers=1)),      # rows of similar length: no split
+    (m.PATTERN_LOGNORMAL, 1.5, m.Config(kernel=2, n_tile=512, acc_buffers=1)),   # rows up to ~13x the mean: split
+    (m.PATTERN_LOGNORMAL, 1.5, m.Config(kernel=2, n_tile=256, acc_buffers=2)),
+])
+def test_plan_headline_size_exact_checksums(dev, pattern, param, cfg):
+    M = K = 16384
+    N, bR = 512, 64
+    rp, ci = m.gen_structure(M, K, bR, pattern, 0.02, param, seed=20240)
+    rng = np.random.default_rng(1)
+    vals = rng.integers(-2, 3, len(ci) * bR * 16).astype(np.float32)
+    B = rng.integers(-2, 3, (K, N)).astype(np.int64)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, m.DType.BF16, device=dev)
+    Bd = torch.from_numpy(B.astype(np.float32)).to(dev).bfloat16()
+    plan = m.BcsrPlan(A, N, cfg)
+    items, groups, pcfg = plan.info()
+    ntiles = -(-N // pcfg.n_tile)
+    if pattern == m.PATTERN_RANDOM:
+        assert groups == 0 and items == (M // bR) * ntiles
+    else:
+        assert groups > 0 and items > (M // bR) * ntiles
+    blocks = vals.reshape(-1, bR, 16).astype(np.int64)
+    bsum = B.sum(axis=1).reshape(K // 16, 16)
+    rows = np.zeros((M // bR, bR), np.int64)
+    np.add.at(rows, np.repeat(np.arange(M // bR), np.diff(rp)), np.einsum("brc,bc->br", blocks, bsum[ci]))
+    colA = np.zeros((K // 16, 16), np.int64)
+    np.add.at(colA, ci, blocks.sum(axis=1))
+    cols = colA.reshape(-1) @ B
+    first = None
+    for run in range(3):   # the split rows' counters reset between launches
+        C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+        plan.run(A, Bd, C=C)
+        m.device_error_check()
+        Ch = C.cpu().double().numpy()
+        assert np.array_equal(Ch.sum(axis=1), rows.reshape(-1).astype(np.float64)), run
+        assert np.array_equal(Ch.sum(axis=0), cols.astype(np.float64)), run
+        if first is None:
+            first = Ch
+        assert np.array_equal(Ch, first)
+    plan.close()
+
+
+@pytest.mark.parametrize("bR,M,K,N,cfg", [
+    (64, 4096, 8192, 264, m.Config(kernel=2, n_tile=256)),          # 2 column tiles, ragged N, spare slots
+    (64, 16384, 4096, 512, m.Config(kernel=2, n_tile=512, acc_buffers=2)),   # one CTA per SM: no spare slots
+    (64, 16384, 4096, 512, m.Config(kernel=2, n_tile=256, acc_buffers=2)),   # 512 items: no spare slots
+    (32, 2048, 4096, 256, None),
+    (16, 1024, 4096, 256, None),
+])
+def test_plan_matches_unplanned_and_fp64(dev, bR, M, K, N, cfg):
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, 0.05, 1.5, seed=M + bR)
+    vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=3)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, m.DType.F16, device=dev)
+    Bd = torch.from_numpy(m.gen_dense(K, N, m.DIST_UNIFORM, seed=4)).to(dev).half()
+    plan = m.BcsrPlan(A, N, cfg)
+    items, split_rows, pcfg = plan.info()
+    C1 = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    for _ in range(2):
+        plan.run(A, Bd, C=C1)
+    C0 = m.spmm(A, Bd, N=N, cfg=pcfg)
+    m.device_error_check()
+    plan.close()
+    got, base = C1.cpu().numpy(), C0.cpu().numpy()
+    assert np.isfinite(got).all()
+    mx, fr = oracle.rel_errors(got, base.astype(np.float64))
+    assert mx <= 1e-5 and fr <= 1e-5, (split_rows, mx, fr)
+    vh = vals.astype(np.float16).astype(np.float64)
+    ref = oracle.bcsr_matmul_f64(rp, ci, vh, bR, 16, Bd.cpu().double().numpy())
+    mx, fr = oracle.rel_errors(got, ref)
+    assert mx <= 2e-5 and fr <= 2e-5
+
+
+def test_plan_rejects(dev):
+    M = K = 1024
+    rp, ci = m.gen_structure(M, K, 64, m.PATTERN_RANDOM, 0.1, 0, seed=1)
+    vals = m.gen_values(len(ci), 64, 16, m.DIST_UNIFORM, seed=2)
+    A = m.BCSR.from_host(M, K, 64, rp, ci, vals, m.DType.F16, device=dev)
+    for cfg in (m.Config(kernel=1), m.Config(kernel=2, split_k=2), m.Config(kernel=2, schedule=1)):
+        with pytest.raises(m.SpmmError) as e:
+            m.BcsrPlan(A, 256, cfg)
+        assert e.value.status == m.Status.UNSUPPORTED
+    plan = m.BcsrPlan(A, 256)
+    rp2, ci2 = m.gen_structure(2 * M, K, 64, m.PATTERN_RANDOM, 0.1, 0, seed=1)
+    A2 = m.BCSR.from_host(2 * M, K, 64, rp2, ci2, m.gen_values(len(ci2), 64, 16, m.DIST_UNIFORM, seed=2),
+                          m.DType.F16, device=dev)
+    B = torch.zeros((K, 256), dtype=torch.float16, device=dev)
+    with pytest.raises(m.SpmmError) as e:
+        plan.run(A2, B, C=torch.empty((2 * M, 256), dtype=torch.float32, device=dev))   # not the plan's M
+    assert e.value.status == m.Status.INVALID_ARG
+    plan.close()
