@@ -95,6 +95,11 @@ __device__ __forceinline__ bool bar_red_or(int id, int nthreads, bool pred) {
   return r != 0;
 }
 
+// C[p] += v at L2 without a returned value (p: a global address).
+__device__ __forceinline__ void red_add_f32(float* p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "f"(v) : "memory");
+}
+
 // ---- TMA -----------------------------------------------------------------------
 // Untiled bulk copy global -> shared (16-byte aligned ends, size % 16 == 0).
 __device__ __forceinline__ void tma_bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,

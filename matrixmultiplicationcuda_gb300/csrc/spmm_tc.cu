@@ -527,7 +527,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                 for (int i = 0; i < 16; ++i) cptr[(long long)(c0 + i) * p.ldc] = v[i];
               } else if (role == 2 || (p.split > 1 && !empty)) {
 #pragma unroll
-                for (int i = 0; i < 16; ++i) atomicAdd(cptr + (long long)(c0 + i) * p.ldc, v[i]);
+                for (int i = 0; i < 16; ++i) red_add_f32(cptr + (long long)(c0 + i) * p.ldc, v[i]);
               } else if (p.split == 1) {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) __stcs(cptr + (long long)(c0 + i) * p.ldc, v[i]);

@@ -20,6 +20,9 @@ Families (seeded synthetic inputs; a few hundred MB on the device at most):
   csr       k_csr_mm on the same matrix's entries, all as CSR
   tc64      k_bcsr_tc64 (64-row blocks, M=64 UMMAs, one CTA per SM): the tc
             product in fp16 and in split fp16, 256-column tile
+  plan      k_bcsr_tc on a per-matrix plan: A 8192^2, 64x16 blocks, log-normal
+            rows (5 %, CV 1.5), N 512, bf16, 256-column tile (rows far above
+            the average load split into parts)
   dense     k_dense_tc: the native dense comparator, A 8192 x 8192, B 8192 x 1024, fp16
   gen       the GPU generators: k_gen_structure + k_gen_values for the tc
             product's structure (A 16384^2, 64x16, 2 %), k_gen_dense for B
@@ -40,7 +43,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr,"
-                                      "tc64,gen,dense")
+                                      "tc64,gen,dense,plan")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args(argv)
     import torch
@@ -153,6 +156,17 @@ def main(argv=None):
         A, B, Blo, bs, C = c3(m.DType.F16_SPLIT)
         run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256), B_lo=Blo))
         print("tc64: nnzb=%d" % A.nnzb)
+    if "plan" in only:
+        M = K = 8192
+        rp, ci = m.gen_structure(M, K, 64, m.PATTERN_LOGNORMAL, 0.05, 1.5, seed=77)
+        vals = m.gen_values(len(ci), 64, 16, m.DIST_UNIFORM, seed=1)
+        A = m.BCSR.from_host(M, K, 64, rp, ci, vals, m.DType.BF16, device=dev)
+        B = torch.from_numpy(m.gen_dense(K, 512, m.DIST_UNIFORM, seed=2)).to(dev).bfloat16()
+        C = torch.empty((M, 512), dtype=torch.float32, device=dev)
+        plan = m.BcsrPlan(A, 512, m.Config(kernel=2, n_tile=256, acc_buffers=2))
+        run(lambda: plan.run(A, B, C=C))
+        print("plan: (items, split rows) =", plan.info()[:2])
+        plan.close()
     if "dense" in only:
         g = torch.Generator().manual_seed(0)
         Ad = (torch.rand((8192, 8192), generator=g) * 2 - 1).half().to(dev)
