@@ -104,3 +104,36 @@ def test_plan_rejects(dev):
         plan.run(A2, B, C=torch.empty((2 * M, 256), dtype=torch.float32, device=dev))   # not the plan's M
     assert e.value.status == m.Status.INVALID_ARG
     plan.close()
+
+
+def test_plan_in_cuda_graph(dev):
+    """plan.run is one launch with no allocation or synchronisation, so it
+    captures into a CUDA graph; replays (split rows included) match eager runs
+    and leave the counters reset."""
+    M = K = 8192
+    N, bR = 512, 64
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_LOGNORMAL, 0.05, 1.5, seed=77)
+    rng = np.random.default_rng(3)
+    vals = rng.integers(-2, 3, len(ci) * bR * 16).astype(np.float32)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, m.DType.F16, device=dev)
+    B = torch.from_numpy(rng.integers(-2, 3, (K, N)).astype(np.float32)).to(dev).half()
+    plan = m.BcsrPlan(A, N, m.Config(kernel=2, n_tile=256, acc_buffers=2))
+    assert plan.info()[1] > 0
+    eager = plan.run(A, B).clone()
+    C = torch.empty((M, N), dtype=torch.float32, device=dev)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.run(A, B, C=C, stream=s)      # warm-up on the capture stream
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.run(A, B, C=C, stream=torch.cuda.current_stream())
+    for _ in range(3):
+        C.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        m.device_error_check()
+        assert torch.equal(C, eager)       # integer inputs: exact whatever the order of the adds
+    plan.close()
