@@ -91,6 +91,7 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   struct Item {
     int4 d;
     int pair;
+    int key;   // heaviness: its blocks, or for a part the longest part of its row
   };
   std::vector<Item> items;
   std::vector<int> group_parts;
@@ -100,21 +101,23 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
     const int k = len > kSplitFactor * avg ? (int)std::min<long long>(kMaxParts, (len + avg - 1) / avg) : 1;
     for (int t = 0; t < ntiles; ++t) {
       if (k == 1) {
-        items.push_back({make_int4(r, t, rp[r], rp[r + 1]), -1});
+        items.push_back({make_int4(r, t, rp[r], rp[r + 1]), -1, len});
         continue;
       }
       const int g = (int)group_parts.size();
       group_parts.push_back(k);
       for (int q = 0; q < k; ++q)
         items.push_back({make_int4(r, t, rp[r] + (int)((long long)len * q / k), rp[r] + (int)((long long)len * (q + 1) / k)),
-                         128 * g + q});
+                         128 * g + q, (len + k - 1) / k});
     }
   }
   const int pairs = (int)group_parts.size();
   if (items.size() >= (1u << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
-  // heaviest first: with more items than CTAs, each CTA's next item is lighter
-  std::stable_sort(items.begin(), items.end(),
-                   [](const Item& a, const Item& b) { return a.d.w - a.d.z > b.d.w - b.d.z; });
+  // Heaviest first: with more items than CTAs, each CTA's next item is lighter.
+  // The parts of a row share one key, so the stable sort keeps part 0 ahead of
+  // its siblings: a CTA takes its items in list order, so every part waits only
+  // for a part 0 earlier in the list, and those waits cannot form a cycle.
+  std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.key > b.key; });
   std::vector<int4> hd(items.size());
   std::vector<int> hp(items.size());
   for (size_t i = 0; i < items.size(); ++i) {

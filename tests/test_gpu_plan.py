@@ -137,3 +137,41 @@ def test_plan_in_cuda_graph(dev):
         m.device_error_check()
         assert torch.equal(C, eager)       # integer inputs: exact whatever the order of the adds
     plan.close()
+
+
+def test_plan_unequal_parts_more_items_than_ctas(dev):
+    """A few rows of 301 blocks among rows of 5, four column tiles: more items
+    than CTAs, and each long row cut into parts of unequal length (23 and 24
+    blocks). Part 0 of a row must come before its siblings in the item list,
+    or a CTA could wait for a zeroing it does itself later. Exact checksums,
+    three launches, no wait gives up."""
+    M = K = 8192
+    N, bR = 1024, 64
+    MB, KB = M // bR, K // 16
+    lens = np.full(MB, 5)
+    lens[[0, 40, 77, 127]] = 301
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    rng = np.random.default_rng(8)
+    ci = np.concatenate([np.sort(rng.choice(KB, n, replace=False)) for n in lens]).astype(np.int32)
+    vals = rng.integers(-2, 3, len(ci) * bR * 16).astype(np.float32)
+    B = rng.integers(-2, 3, (K, N)).astype(np.int64)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, m.DType.F16, device=dev)
+    Bd = torch.from_numpy(B.astype(np.float32)).to(dev).half()
+    plan = m.BcsrPlan(A, N, m.Config(kernel=2, n_tile=256, acc_buffers=2))
+    items, groups, _ = plan.info()
+    assert groups == 4 * 4 and items > 304
+    blocks = vals.reshape(-1, bR, 16).astype(np.int64)
+    bsum = B.sum(axis=1).reshape(K // 16, 16)
+    rows = np.zeros((MB, bR), np.int64)
+    np.add.at(rows, np.repeat(np.arange(MB), lens), np.einsum("brc,bc->br", blocks, bsum[ci]))
+    colA = np.zeros((K // 16, 16), np.int64)
+    np.add.at(colA, ci, blocks.sum(axis=1))
+    cols = colA.reshape(-1) @ B
+    for run in range(3):
+        C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+        plan.run(A, Bd, C=C)
+        m.device_error_check()
+        Ch = C.cpu().double().numpy()
+        assert np.array_equal(Ch.sum(axis=1), rows.reshape(-1).astype(np.float64)), run
+        assert np.array_equal(Ch.sum(axis=0), cols.astype(np.float64)), run
+    plan.close()
