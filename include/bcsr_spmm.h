@@ -338,10 +338,15 @@ spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr
  * average load per CTA slot is cut into parts of about that load, run by
  * different CTAs: part 0 zeroes the row's C tile while its MMAs run, and
  * every part adds its tile into C with red.add (so C of those rows is summed
- * in an order that varies from run to run within fp32 rounding). _run is one
- * launch; A must have the plan's M, K, block shape, dtype and row_ptr (column
- * indices and values may differ), and N must be the plan's. One plan runs
- * one launch at a time. cfg: kernel 0 or 2, no split-K, static schedule.
+ * in an order that varies from run to run within fp32 rounding). The CTAs
+ * take the items from the plan's own work queue, each claiming its next item
+ * shortly before it has copied the current one, so that CTAs that run faster
+ * take more of the lighter items at the end of the list. _run is one launch;
+ * A must have the plan's M, K, block shape, dtype and row_ptr (column indices
+ * and values may differ), and N must be the plan's. One plan runs one launch
+ * at a time (its queue and counters are its own; use one plan per stream for
+ * concurrent launches). cfg: kernel 0 or 2, no split-K, schedule 0 or 1
+ * (either way the plan's own queue; _info reports schedule 1).
  * spmm_bcsr_plan_info: item count, split rows (row and column-tile pairs),
  * and the configuration the plan runs. */
 typedef struct spmm_bcsr_plan spmm_bcsr_plan;

@@ -125,8 +125,10 @@ def hcsr_mm(A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, B, N=None, C=Non
 class BcsrPlan:
     """A per-matrix plan for the tcgen05 pipeline (spmm_bcsr_plan_*): the item
     list ordered heaviest first, with the longest block rows split across the
-    CTA slots the rows leave spare. Built once from A's row_ptr; run() is one
-    launch on any A with the same structure."""
+    CTA slots the rows leave spare, taken by the CTAs from the plan's own work
+    queue. Built once from A's row_ptr; run() is one launch on any A with the
+    same structure. One plan runs one launch at a time: use one plan per
+    stream for concurrent launches."""
 
     def __init__(self, A: BCSR, N, cfg: Optional[Config] = None, stream=None):
         a = A.desc()

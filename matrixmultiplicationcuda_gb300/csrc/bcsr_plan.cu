@@ -1,5 +1,6 @@
 // A per-matrix plan for the tcgen05 pipeline: an item list ordered heaviest
-// first, with block rows far longer than the rest split into parts.
+// first, with block rows far longer than the rest split into parts, taken by
+// the CTAs from the plan's own work queue.
 //
 // A launch of k_bcsr_tc is bound by its longest CTA: one item is a block row
 // (and column tile), and a CTA streams its blocks at a fixed rate, so a row
@@ -10,6 +11,12 @@
 // with red.add once that is done. Rows not split store C directly, as without
 // a plan; on rows of similar lengths (no row that long) the plan only orders
 // the items.
+//
+// Each CTA starts on item blockIdx.x and takes every later item from the
+// queue shortly before it has copied the current one, so CTAs that run faster
+// (lighter items, or an SM they no longer share) take more of the lighter
+// items at the end of the list. Claims follow list order, and so does each
+// CTA's own sequence of items.
 //
 // The plan holds only what row_ptr determines: any A with the same M, K, block
 // shape, dtype and row_ptr (values and column indices may change) runs on it.
@@ -28,7 +35,8 @@ struct spmm_bcsr_plan {
   int4* items = nullptr;       // {block row, column tile, first block, end block}
   int* pair = nullptr;         // -1, or 128 * group + part
   int* parts = nullptr;        // parts per group (split row and tile)
-  unsigned* counters = nullptr;   // per group: {C tile zeroed, parts finished}
+  unsigned* counters = nullptr;   // per group: {C tile zeroed, parts finished}; then the queue
+  unsigned* queue = nullptr;      // {next ticket, CTAs done}, inside `counters`
 };
 
 namespace spmm {
@@ -67,9 +75,10 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   std::memset(&c, 0, sizeof(c));
   if (cfg) c = *cfg;
   if (c.kernel != 0 && c.kernel != 2) return fail(SPMM_ERR_UNSUPPORTED, "a plan runs on kernel 2");
-  if (c.split_k > 1 || c.schedule != 0)
-    return fail(SPMM_ERR_UNSUPPORTED, "a plan replaces split-K and the work queue");
+  if (c.split_k > 1 || (c.schedule != 0 && c.schedule != 1))
+    return fail(SPMM_ERR_UNSUPPORTED, "a plan replaces split-K and brings its own work queue");
   c.kernel = 2;
+  c.schedule = 1;   // the plan's queue
   int nt = 0, per_sm = 0;
   if (!tc_geometry(A->bR, A->dtype, N, c, &nt, &per_sm))
     return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for this block height, dtype and configuration");
@@ -136,17 +145,18 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   if (cudaMalloc(&p->items, sizeof(int4) * hd.size()) != cudaSuccess ||
       cudaMalloc(&p->pair, sizeof(int) * hp.size()) != cudaSuccess ||
       cudaMalloc(&p->parts, sizeof(int) * std::max(pairs, 1)) != cudaSuccess ||
-      cudaMalloc(&p->counters, sizeof(unsigned) * 2 * std::max(pairs, 1)) != cudaSuccess) {
+      cudaMalloc(&p->counters, sizeof(unsigned) * (2 * std::max(pairs, 1) + 2)) != cudaSuccess) {
     plan_free(p);
     return fail(SPMM_ERR_CUDA, "plan allocation failed");
   }
   if (cudaMemcpy(p->items, hd.data(), sizeof(int4) * hd.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(p->pair, hp.data(), sizeof(int) * hp.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       (pairs > 0 && cudaMemcpy(p->parts, group_parts.data(), sizeof(int) * pairs, cudaMemcpyHostToDevice) != cudaSuccess) ||
-      cudaMemset(p->counters, 0, sizeof(unsigned) * 2 * std::max(pairs, 1)) != cudaSuccess) {
+      cudaMemset(p->counters, 0, sizeof(unsigned) * (2 * std::max(pairs, 1) + 2)) != cudaSuccess) {
     plan_free(p);
     return fail(SPMM_ERR_CUDA, "plan upload failed");
   }
+  p->queue = p->counters + 2 * std::max(pairs, 1);
   *out = p;
   return SPMM_OK;
 }
@@ -183,6 +193,7 @@ extern "C" spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* p, const spmm_bc
   r.parts = p->parts;
   r.counters = p->counters;
   r.plan_items = p->n_items;
+  r.queue = p->queue;
   return launch_tc(r);
 }
 

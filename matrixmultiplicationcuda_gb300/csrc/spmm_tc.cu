@@ -18,8 +18,9 @@
 //     in the K-major canonical layout (8-row groups 256 B apart); the blocks
 //     of a group are contiguous in memory and arrive in one copy.
 //
-// Warp roles (10 warps, two CTAs per SM): warp 0 takes items (static stride
-// or work queue), publishes them through an item ring and copies A groups;
+// Warp roles (10 warps, two CTAs per SM): warp 0 takes items (static stride,
+// or from a work queue a few groups before the current item is copied),
+// publishes them through an item ring and copies A groups;
 // warps 2, 3, 8, 9 copy the B panels (a TMA instruction holds its issuing
 // thread for ~200 ns, so four threads share them); warp 1 (one thread) issues
 // the UMMAs, releases each group's ring slot with tcgen05.commit and hands
@@ -54,6 +55,7 @@ struct TcParams {
   unsigned* err;
   int panel3d;      // B panel loaded by one 3-D copy (N % 64 == 0)
   unsigned* queue;  // [0] next item, [1] CTAs done; NULL = static item striding
+  int claim_ahead;  // work queue: claim the next item when this many groups of the current one are left to copy
   int split;        // items per (block row, column tile); > 1: partial sums added into C
   // hybrid (BCSR + CSR): the CSR part's entries are added in the epilogue
   // (NULL csr_row_ptr = plain BCSR)
@@ -141,8 +143,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const uint32_t tfull0 = empty0 + 8 * STAGES, tempty0 = tfull0 + 16, done_bar = tempty0 + 16;
   const uint32_t qfull0 = done_bar + 8, qempty0 = qfull0 + 8 * kQ;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5 + 2 * kQ);
-  int* s_item = reinterpret_cast<int*>(tmem_slot + 1);      // kQ x {item, start, end}
-  int* s_role = s_item + 3 * kQ;                            // a split row's role, set by the epilogue
+  int* s_item = reinterpret_cast<int*>(tmem_slot + 1);      // kQ x {item, start, end, column tile}
+  int* s_role = s_item + 4 * kQ;                            // a split row's role, set by the epilogue
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 32) {
@@ -168,6 +170,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  // A CTA's first item is blockIdx.x (the grid never exceeds the item count).
+  // A plan's item list is the library's own, written when the plan was made,
+  // so its first entry is read before the wait for the previous kernel in the
+  // stream; everything the caller passes is read after it.
+  int4 first = make_int4(0, 0, 0, 0);
+  if (warp == 0 && lane == 0 && p.items) first = __ldg(p.items + blockIdx.x);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -176,15 +184,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   grid_dep_wait();
 
   // Ring entry `it` of the item stream (bounded wait); *item < 0 ends the stream.
-  auto read_item = [&](uint32_t it, int* item, int* start, int* end, unsigned code) -> bool {
+  auto read_item = [&](uint32_t it, int* item, int* start, int* end, unsigned code, int* tile = nullptr) -> bool {
     const uint32_t q = it % kQ;
     if (!mbar_wait(qfull0 + 8 * q, (it / kQ) & 1, p.timeout_ns)) {
       atomicOr(p.err, code);
       return false;
     }
-    *item = s_item[3 * q];
-    *start = s_item[3 * q + 1];
-    *end = s_item[3 * q + 2];
+    *item = s_item[4 * q];
+    *start = s_item[4 * q + 1];
+    *end = s_item[4 * q + 2];
+    if (tile) *tile = s_item[4 * q + 3];
     mbar_arrive(qempty0 + 8 * q);
     return true;
   };
@@ -200,26 +209,24 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       tma_prefetch_desc(&tmAg);
       tma_prefetch_desc(&tmA1);
       const uint64_t pol_a = l2_policy_evict_first();
-      auto next_item = [&](int cur) -> int {
-        int v = p.queue ? (int)atomicAdd(p.queue, 1u) : (cur < 0 ? (int)blockIdx.x : cur + (int)gridDim.x);
-        return v < p.n_items ? v : -1;
-      };
       uint32_t gs = 0, it = 0;
       bool failed = false;
-      // block range of an item: its block row's range, or one of p.split
-      // slices of it (slice lengths a multiple of 4 blocks, so that only a
-      // row's last slice can end in a partial group)
-      auto range = [&](int v, int* s0, int* s1) {
+      // block range and column tile of an item: its block row's range, or one
+      // of p.split slices of it (slice lengths a multiple of 4 blocks, so that
+      // only a row's last slice can end in a partial group)
+      auto range = [&](int v, int* s0, int* s1, int* tile) {
         if (v < 0) {
-          *s0 = *s1 = 0;
+          *s0 = *s1 = *tile = 0;
           return;
         }
         if (p.items) {
           const int4 d = __ldg(p.items + v);
           *s0 = d.z;
           *s1 = d.w;
+          *tile = d.y;
           return;
         }
+        *tile = (v / p.split) % p.ntiles;
         const int row = v / (p.ntiles * p.split);
         int a = __ldg(p.row_ptr + row), b = __ldg(p.row_ptr + row + 1);
         if (p.split > 1) {
@@ -232,24 +239,68 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         *s0 = a;
         *s1 = b;
       };
-      int item = next_item(-1);
-      int start = 0, end = 0;
-      range(item, &start, &end);
-      for (;; ++it) {
-        const uint32_t q = it % kQ;
-        if (it >= (uint32_t)kQ && !mbar_wait(qempty0 + 8 * q, ((it / kQ) + 1) & 1, p.timeout_ns)) {
+      // ring entry `e` := (v, s0, s1, tile); a wait for the slot that gives up ends the stream
+      auto publish = [&](uint32_t e, int v, int s0, int s1, int tile) {
+        const uint32_t q = e % kQ;
+        if (e >= (uint32_t)kQ && !mbar_wait(qempty0 + 8 * q, ((e / kQ) + 1) & 1, p.timeout_ns)) {
           atomicOr(p.err, 4u);
           failed = true;
         }
-        s_item[3 * q] = failed ? -1 : item;
-        s_item[3 * q + 1] = start;
-        s_item[3 * q + 2] = end;
+        s_item[4 * q] = failed ? -1 : v;
+        s_item[4 * q + 1] = s0;
+        s_item[4 * q + 2] = s1;
+        s_item[4 * q + 3] = tile;
         mbar_arrive(qfull0 + 8 * q);
+      };
+      // Items after the first: static striding (blockIdx.x + k * gridDim.x),
+      // or tickets from the work queue offset by the grid size. A ticket is
+      // taken late, when claim_ahead groups of the current item are left to
+      // copy (< 0: as the item starts), so that a CTA running faster (lighter
+      // items, or an SM it no longer shares) takes more of the items still
+      // unclaimed; its atomic is issued one group before the result is used,
+      // and the item goes into the ring at once. Either way every CTA takes
+      // its items in increasing list order.
+      const bool late = p.queue != nullptr && p.claim_ahead >= 0;
+      auto ticket_item = [&](unsigned t) -> int {
+        const unsigned v = t + gridDim.x;
+        return v < (unsigned)p.n_items ? (int)v : -1;
+      };
+      int item = (int)blockIdx.x;
+      int start = 0, end = 0, tile = 0;
+      if (p.items) {
+        start = first.z;
+        end = first.w;
+        tile = first.y;
+      } else {
+        range(item, &start, &end, &tile);
+      }
+      bool in_ring = false;
+      for (;; ++it) {
+        if (!in_ring) publish(it, item, start, end, tile);
         if (item < 0 || failed) break;
-        const int nitem = next_item(item);
-        int nstart = 0, nend = 0;
-        range(nitem, &nstart, &nend);
-        for (int j0 = start; j0 < end; j0 += G, ++gs) {
+        int nitem = -2, nstart = 0, nend = 0, ntile = 0;
+        bool claimed = false;
+        unsigned ticket = 0;
+        if (!late) {
+          // the next item's indices load now and are used once this item is copied
+          nitem = p.queue ? ticket_item(atomicAdd(p.queue, 1u))
+                          : (item + (int)gridDim.x < p.n_items ? item + (int)gridDim.x : -1);
+          range(nitem, &nstart, &nend, &ntile);
+        }
+        const int ngroups = (end - start + G - 1) / G;
+        int gi = 0;
+        for (int j0 = start; j0 < end; j0 += G, ++gs, ++gi) {
+          if (late && nitem == -2) {
+            if (claimed) {
+              nitem = ticket_item(ticket);
+              range(nitem, &nstart, &nend, &ntile);
+              publish(it + 1, nitem, nstart, nend, ntile);
+              if (failed) break;
+            } else if (ngroups - gi <= p.claim_ahead + 1) {
+              ticket = atomicAdd(p.queue, 1u);
+              claimed = true;
+            }
+          }
           const int n = min(G, end - j0);
           const int s = (int)(gs % STAGES);
           if (gs >= (uint32_t)STAGES && !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
@@ -274,9 +325,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           }
         }
         if (failed) break;
+        in_ring = late && nitem != -2;
+        if (nitem == -2) {   // late claim not made or not used yet (short item)
+          if (!claimed) ticket = atomicAdd(p.queue, 1u);
+          nitem = ticket_item(ticket);
+          range(nitem, &nstart, &nend, &ntile);
+        }
         item = nitem;
         start = nstart;
         end = nend;
+        tile = ntile;
       }
       // the last CTA to finish resets the queue for the next launch
       if (p.queue) {
@@ -300,14 +358,14 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     uint32_t gs = 0;
     int failed = 0;
     for (uint32_t it = 0; !failed; ++it) {
-      int item = -1, start = 0, end = 0, ok = 1;
-      if (lane == 0) ok = read_item(it, &item, &start, &end, 4u) ? 1 : 0;
+      int item = -1, start = 0, end = 0, nt = 0, ok = 1;
+      if (lane == 0) ok = read_item(it, &item, &start, &end, 4u, &nt) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       item = __shfl_sync(0xffffffffu, item, 0);
       start = __shfl_sync(0xffffffffu, start, 0);
       end = __shfl_sync(0xffffffffu, end, 0);
+      nt = __shfl_sync(0xffffffffu, nt, 0);
       if (!ok || item < 0) break;
-      const int nt = p.items ? __ldg(&p.items[item].y) : (item / p.split) % p.ntiles;
       int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
@@ -583,9 +641,14 @@ struct TcEntry {
 
 // Instantiated (block height, column tile, ring depth in groups, accumulators,
 // group size) per type.
-// The first entry of a (block height, column tile) pair is its default.
+// The first entry of a (block height, column tile) pair is its default. For
+// 64-row blocks and 256 columns that is a ring of five 2-block groups (2 x 103
+// KB of shared memory per SM): the pipeline is bound by the latency of its
+// copies, and the fifth group measured ~2 % faster than four on the headline
+// product.
 #define SPMM_TC_SHAPES(MODE)                                                                         \
-  SPMM_TC_ENTRY(64, 256, 4, MODE, 2, 2), SPMM_TC_ENTRY(64, 256, 2, MODE, 2, 4),                     \
+  SPMM_TC_ENTRY(64, 256, 5, MODE, 2, 2), SPMM_TC_ENTRY(64, 256, 4, MODE, 2, 2),                     \
+      SPMM_TC_ENTRY(64, 256, 2, MODE, 2, 4),                                                        \
       SPMM_TC_ENTRY(64, 512, 3, MODE, 1, 2), SPMM_TC_ENTRY(64, 512, 3, MODE, 2, 4),                 \
       SPMM_TC_ENTRY(64, 128, 4, MODE, 2, 4), SPMM_TC_ENTRY(32, 256, 3, MODE, 2, 4),                 \
       SPMM_TC_ENTRY(32, 512, 3, MODE, 1, 2), SPMM_TC_ENTRY(16, 256, 3, MODE, 2, 4),                 \
@@ -721,6 +784,7 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.panel3d = panel3d;
   // items: static stride by default, or a work queue on request
   p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
+  p.claim_ahead = e->stages - 1;
   p.csr_row_ptr = r.csr ? r.csr->row_ptr : nullptr;
   p.csr_col_idx = r.csr ? r.csr->col_idx : nullptr;
   p.csr_vals = r.csr ? static_cast<const __half*>(r.csr->vals) : nullptr;
@@ -732,8 +796,8 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.parts = r.parts;
   p.counters = r.counters;
   if (r.items) {
-    if (p.split > 1 || r.csr || r.gather_rows || p.queue)
-      return fail(SPMM_ERR_UNSUPPORTED, "a planned product runs without split-K, CSR part or work queue");
+    if (p.split > 1 || r.csr || r.gather_rows || (p.queue && !r.queue))
+      return fail(SPMM_ERR_UNSUPPORTED, "a planned product runs without split-K, CSR part or shared work queue");
     p.n_items = r.plan_items;
   }
   if (r.csr && (p.split > 1 || mode != MODE_F16))

@@ -450,7 +450,8 @@ class Runner {
       r.tuning = tuning;
       if (tuning == "plan") {
         // the per-matrix plan on the tcgen05 pipeline: the model's configuration
-        // when it runs there (without split-K or the work queue), else its default
+        // when it runs there (without split-K; the plan brings its own work
+        // queue), else its default
         spmm_config mc{};
         if (model_) SK(spmm_cost_model_select(model_, &P.A, P.N, &mc, nullptr, nullptr));
         if (mc.kernel == 2) {
