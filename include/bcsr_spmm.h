@@ -355,6 +355,18 @@ spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, const spmm_con
 spmm_status spmm_bcsr_plan_info(const spmm_bcsr_plan* plan, int* items, int* split_rows, spmm_config* cfg);
 spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* plan, const spmm_bcsr_desc* A, const spmm_dense_desc* B,
                                int N, float* C, int ldc, void* stream);
+/* _run with flags (_run is _run_ex with flags 0).
+ * SPMM_RUN_INPUTS_READY: the caller promises that no kernel launched on
+ *   `stream` since the stream was last synchronised with the host writes A's
+ *   arrays or B (constant operands, or a sequence of independent products
+ *   whose inputs were all prepared first). The launch may then copy and
+ *   multiply its first items while the kernel before it on the stream is
+ *   still running (programmatic dependent launch); it still waits for that
+ *   kernel before it claims work from the plan's queue and before it writes
+ *   C. Without the promise the flag may read stale A or B. */
+#define SPMM_RUN_INPUTS_READY 1u
+spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* plan, const spmm_bcsr_desc* A, const spmm_dense_desc* B,
+                                  int N, float* C, int ldc, unsigned flags, void* stream);
 spmm_status spmm_bcsr_plan_destroy(spmm_bcsr_plan* plan);
 
 /* ---- allocation-free variant ---------------------------------------------------

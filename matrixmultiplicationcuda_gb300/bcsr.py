@@ -122,6 +122,9 @@ def hcsr_mm(A_blocks: BCSR, csr_row_ptr, csr_col_idx, csr_vals, B, N=None, C=Non
     return C
 
 
+RUN_INPUTS_READY = 1   # SPMM_RUN_INPUTS_READY
+
+
 class BcsrPlan:
     """A per-matrix plan for the tcgen05 pipeline (spmm_bcsr_plan_*): the item
     list ordered heaviest first, with the longest block rows split across the
@@ -144,15 +147,21 @@ class BcsrPlan:
         check(lib().spmm_bcsr_plan_info(self._h, ctypes.byref(n), ctypes.byref(sp), ctypes.byref(c)))
         return n.value, sp.value, c
 
-    def run(self, A: BCSR, B, C=None, stream=None, B_lo=None, b_scale=1.0, ldc=None):
+    def run(self, A: BCSR, B, C=None, stream=None, B_lo=None, b_scale=1.0, ldc=None, inputs_ready=False):
+        """One launch. inputs_ready=True (SPMM_RUN_INPUTS_READY) promises that no
+        kernel launched on the stream since its last host synchronisation writes A
+        or B: the launch then copies and multiplies its first items while the kernel
+        before it is still running, and waits for that kernel only before it claims
+        queued work or writes C."""
         torch = _torch()
         if C is None:
             C = torch.empty((self.M, self.N), dtype=torch.float32, device=B.device)
         ldc = int(C.stride(0)) if ldc is None else int(ldc)
         a = A.desc()
         b = _dense_desc(B, B_lo, b_scale, ldb=B.stride(0))
-        check(lib().spmm_bcsr_plan_run(self._h, ctypes.byref(a), ctypes.byref(b), self.N,
-                                       ctypes.c_void_p(C.data_ptr()), ldc, stream_handle(stream)))
+        check(lib().spmm_bcsr_plan_run_ex(self._h, ctypes.byref(a), ctypes.byref(b), self.N,
+                                          ctypes.c_void_p(C.data_ptr()), ldc, RUN_INPUTS_READY if inputs_ready else 0,
+                                          stream_handle(stream)))
         return C
 
     def close(self):

@@ -171,7 +171,14 @@ extern "C" spmm_status spmm_bcsr_plan_info(const spmm_bcsr_plan* p, int* items, 
 
 extern "C" spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* p, const spmm_bcsr_desc* A, const spmm_dense_desc* B,
                                           int N, float* C, int ldc, void* stream) {
+  return spmm_bcsr_plan_run_ex(p, A, B, N, C, ldc, 0u, stream);
+}
+
+extern "C" spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* p, const spmm_bcsr_desc* A,
+                                             const spmm_dense_desc* B, int N, float* C, int ldc, unsigned flags,
+                                             void* stream) {
   if (!p || !A || !B) return fail(SPMM_ERR_INVALID_ARG, "null plan or descriptor");
+  if (flags & ~SPMM_RUN_INPUTS_READY) return fail(SPMM_ERR_INVALID_ARG, "unknown run flags");
   if (A->M != p->M || A->K != p->K || A->bR != p->bR || A->dtype != p->dtype || N != p->N)
     return fail(SPMM_ERR_INVALID_ARG, "A and N must match the plan");
   if (!A->row_ptr || !C || !B->data) return fail(SPMM_ERR_INVALID_ARG, "null pointer");
@@ -194,6 +201,7 @@ extern "C" spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* p, const spmm_bc
   r.counters = p->counters;
   r.plan_items = p->n_items;
   r.queue = p->queue;
+  r.inputs_ready = (flags & SPMM_RUN_INPUTS_READY) != 0;
   return launch_tc(r);
 }
 

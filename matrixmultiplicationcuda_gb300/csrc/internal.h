@@ -88,6 +88,10 @@ struct LaunchRequest {
   const int* parts = nullptr;
   unsigned* counters = nullptr;
   int plan_items = 0;
+  // no kernel launched on the stream since its last host synchronisation
+  // writes A or B: the pipeline's copies and MMAs may start before the
+  // previous kernel has finished (plans only)
+  bool inputs_ready = false;
 };
 // The tcgen05 pipeline's column tile and CTAs per SM for a product (false when
 // it has no kernel for it): what a plan builds its item list for.

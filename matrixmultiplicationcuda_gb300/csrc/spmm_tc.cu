@@ -56,6 +56,7 @@ struct TcParams {
   int panel3d;      // B panel loaded by one 3-D copy (N % 64 == 0)
   unsigned* queue;  // [0] next item, [1] CTAs done; NULL = static item striding
   int claim_ahead;  // work queue: claim the next item when this many groups of the current one are left to copy
+  int inputs_ready; // no kernel earlier on the stream writes A or B (see the dependency wait below)
   int split;        // items per (block row, column tile); > 1: partial sums added into C
   // hybrid (BCSR + CSR): the CSR part's entries are added in the epilogue
   // (NULL csr_row_ptr = plain BCSR)
@@ -181,7 +182,18 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   grid_dep_launch_dependents();
-  grid_dep_wait();
+  // The wait for the previous kernel on the stream (programmatic dependent
+  // launch). With inputs_ready the caller promises that no kernel launched on
+  // the stream since its last host synchronisation writes A or B, so the
+  // warps that read only A and B or work in
+  // shared memory and TMEM (lead, MMA, B issuers) start at once: a CTA copies
+  // and multiplies its first item while the previous kernel finishes. The lead
+  // waits before its first work-queue claim and the epilogue before it touches
+  // C or a split row's counters, so the queue, the counters and C keep their
+  // order with the previous kernel.
+  const bool early = p.inputs_ready && (warp <= 3 || warp == 8 || warp == 9);
+  if (!early) grid_dep_wait();
+  bool dep_waited = !early;
 
   // Ring entry `it` of the item stream (bounded wait); *item < 0 ends the stream.
   auto read_item = [&](uint32_t it, int* item, int* start, int* end, unsigned code, int* tile = nullptr) -> bool {
@@ -283,6 +295,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         unsigned ticket = 0;
         if (!late) {
           // the next item's indices load now and are used once this item is copied
+          if (p.queue && !dep_waited) {
+            grid_dep_wait();
+            dep_waited = true;
+          }
           nitem = p.queue ? ticket_item(atomicAdd(p.queue, 1u))
                           : (item + (int)gridDim.x < p.n_items ? item + (int)gridDim.x : -1);
           range(nitem, &nstart, &nend, &ntile);
@@ -297,6 +313,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
               publish(it + 1, nitem, nstart, nend, ntile);
               if (failed) break;
             } else if (ngroups - gi <= p.claim_ahead + 1) {
+              if (!dep_waited) {
+                grid_dep_wait();
+                dep_waited = true;
+              }
               ticket = atomicAdd(p.queue, 1u);
               claimed = true;
             }
@@ -327,7 +347,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         if (failed) break;
         in_ring = late && nitem != -2;
         if (nitem == -2) {   // late claim not made or not used yet (short item)
-          if (!claimed) ticket = atomicAdd(p.queue, 1u);
+          if (!claimed) {
+            if (!dep_waited) {
+              grid_dep_wait();
+              dep_waited = true;
+            }
+            ticket = atomicAdd(p.queue, 1u);
+          }
           nitem = ticket_item(ticket);
           range(nitem, &nstart, &nend, &ntile);
         }
@@ -338,6 +364,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
       // the last CTA to finish resets the queue for the next launch
       if (p.queue) {
+        if (!dep_waited) grid_dep_wait();
         __threadfence();
         if (atomicAdd(p.queue + 1, 1u) == gridDim.x - 1) {
           p.queue[0] = 0;
@@ -785,6 +812,7 @@ spmm_status launch_tc(const LaunchRequest& r) {
   // items: static stride by default, or a work queue on request
   p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
   p.claim_ahead = e->stages - 1;
+  p.inputs_ready = r.inputs_ready ? 1 : 0;
   p.csr_row_ptr = r.csr ? r.csr->row_ptr : nullptr;
   p.csr_col_idx = r.csr ? r.csr->col_idx : nullptr;
   p.csr_vals = r.csr ? static_cast<const __half*>(r.csr->vals) : nullptr;

@@ -3,8 +3,11 @@
     python -m matrixmultiplicationcuda_gb300.profile_kernels [--only NAME,...] [--launches 3]
 
 Families (seeded synthetic inputs; a few hundred MB on the device at most):
-  tc        k_bcsr_tc: A 16384^2, 64x16 blocks, random 2 %, N 512, fp16, the
-            cost model's configuration (512-column tile, one accumulator)
+  tc        k_bcsr_tc: A 16384^2, 64x16 blocks, random 2 %, N 512, fp16, a
+            512-column tile with one accumulator, static item stride
+  plan_c3   k_bcsr_tc on a per-matrix plan: the same product in bf16 with the
+            default tcgen05 configuration (256-column tile, five-group ring,
+            two accumulators), items heaviest first from the plan's queue
   tc_split  k_bcsr_tc in split fp16 (three MMAs per block), same product
   mma_e4m3  k_bcsr_mma: the same product in e4m3 with per-block scales
   mma16     k_bcsr_mma: A 8192^2, 16x16 blocks, random 5 %, N 1024, fp16
@@ -43,7 +46,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr,"
-                                      "tc64,gen,dense,plan")
+                                      "tc64,gen,dense,plan,plan_c3")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args(argv)
     import torch
@@ -150,6 +153,12 @@ def main(argv=None):
             rh, rx, rd = t(rh), t(rx), t(rd.view(np.float16))
             run(lambda: m.csr_mm(rh, rx, rd, K, B, N=N, C=C))
             print("csr: %d entries" % rx.numel())
+    if "plan_c3" in only:
+        A, B, Blo, bs, C = c3(m.DType.BF16)
+        plan = m.BcsrPlan(A, 512)
+        run(lambda: plan.run(A, B, C=C))
+        print("plan_c3: nnzb=%d, (items, split rows) = %s" % (A.nnzb, plan.info()[:2]))
+        plan.close()
     if "tc64" in only:
         A, B, Blo, bs, C = c3(m.DType.F16)
         run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256)))

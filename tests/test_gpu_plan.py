@@ -177,3 +177,81 @@ def test_plan_unequal_parts_more_items_than_ctas(dev):
         assert np.array_equal(Ch.sum(axis=1), rows.reshape(-1).astype(np.float64)), run
         assert np.array_equal(Ch.sum(axis=0), cols.astype(np.float64)), run
     plan.close()
+
+
+def _int_problem(M, K, N, bR, pattern, density, seed, dev, dtype=m.DType.BF16):
+    rp, ci = m.gen_structure(M, K, bR, pattern, density, 1.5, seed=seed)
+    rng = np.random.default_rng(seed)
+    vals = rng.integers(-2, 3, len(ci) * bR * 16).astype(np.float32)
+    B = rng.integers(-2, 3, (K, N)).astype(np.float32)
+    A = m.BCSR.from_host(M, K, bR, rp, ci, vals, dtype, device=dev)
+    tdt = torch.bfloat16 if dtype == m.DType.BF16 else torch.float16
+    return A, torch.from_numpy(B).to(dev).to(tdt)
+
+
+@pytest.mark.parametrize("pattern,density", [(m.PATTERN_RANDOM, 0.02), (m.PATTERN_LOGNORMAL, 0.05)])
+def test_plan_inputs_ready_back_to_back(dev, pattern, density):
+    """SPMM_RUN_INPUTS_READY over a stream of independent products (four
+    problems with the same structure, different values, round-robin): each
+    launch overlaps the tail of the one before it, claims its queued items and
+    writes C only after that launch has finished. Integer inputs make every
+    product exact, so each C must equal the same product run without the flag,
+    split rows included, over many launches of one plan."""
+    M = K = 16384 if pattern == m.PATTERN_RANDOM else 8192
+    N = 512
+    probs = []
+    for s in range(4):
+        A, B = _int_problem(M, K, N, 64, pattern, density, 31, dev)
+        if s:   # same structure, different values: scale B
+            B = (B * (s + 1)).contiguous()
+        probs.append((A, B))
+    plan = m.BcsrPlan(probs[0][0], N)
+    assert (plan.info()[1] > 0) == (pattern == m.PATTERN_LOGNORMAL)
+    refs = []
+    for A, B in probs:
+        refs.append(plan.run(A, B).clone())
+    Cs = [torch.full((M, N), float("nan"), dtype=torch.float32, device=dev) for _ in probs]
+    torch.cuda.synchronize()   # the flag's promise: no kernel since then writes A or B
+    for i in range(40):
+        A, B = probs[i % 4]
+        plan.run(A, B, C=Cs[i % 4], inputs_ready=True)
+    torch.cuda.synchronize()
+    m.device_error_check()
+    for C, ref in zip(Cs, refs):
+        assert torch.equal(C, ref)
+    plan.close()
+
+
+def test_plan_inputs_ready_keeps_c_order(dev):
+    """Two launches write the same C: the second (with the flag) starts its
+    copies and MMAs while the first runs, but stores C only after the first has
+    finished, so C holds the second product."""
+    M = K = 16384
+    N = 512
+    A1, B1 = _int_problem(M, K, N, 64, m.PATTERN_RANDOM, 0.02, 5, dev)
+    B2 = (B1 * -3).contiguous()
+    plan = m.BcsrPlan(A1, N)
+    ref2 = plan.run(A1, B2).clone()
+    C = torch.empty((M, N), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()   # the flag's promise: no kernel since then writes A or B
+    for _ in range(5):
+        plan.run(A1, B1, C=C)
+        plan.run(A1, B2, C=C, inputs_ready=True)
+        torch.cuda.synchronize()
+        m.device_error_check()
+        assert torch.equal(C, ref2)
+    plan.close()
+
+
+def test_plan_run_rejects_unknown_flags(dev):
+    import ctypes
+    from matrixmultiplicationcuda_gb300._lib import lib, stream_handle
+    from matrixmultiplicationcuda_gb300.bcsr import _dense_desc
+    A, B = _int_problem(1024, 1024, 256, 64, m.PATTERN_RANDOM, 0.1, 2, dev)
+    plan = m.BcsrPlan(A, 256)
+    C = torch.empty((1024, 256), dtype=torch.float32, device=dev)
+    a, b = A.desc(), _dense_desc(B, ldb=B.stride(0))
+    st = lib().spmm_bcsr_plan_run_ex(plan._h, ctypes.byref(a), ctypes.byref(b), 256, ctypes.c_void_p(C.data_ptr()),
+                                     256, 2, stream_handle(None))
+    assert st == int(m.Status.INVALID_ARG)
+    plan.close()
