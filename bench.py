@@ -428,6 +428,7 @@ def run_ours(args, world, rank, local):
         # tcgen05 configuration of the tuner's table without split-K; the
         # fastest plan runs when it beats the model's pick
         plan, t_plan, plan_sweep = None, None, {}
+        cands = {cfg_name(cfg_model): cfg_model, cfg_name(cfg_sweep): cfg_sweep}
         for c in table:
             if c.kernel != 2 or c.split_k > 1 or c.schedule != 0:
                 continue
@@ -438,19 +439,16 @@ def run_ours(args, world, rank, local):
             time_loop(probs, pl, 3)
             t = time_loop(probs, pl, 30)
             plan_sweep[cfg_name(pl)] = t
+            cands[cfg_name(pl)] = pl
             if t_plan is None or t < t_plan:
-                if plan is not None:
-                    plan.close()
                 plan, t_plan = pl, t
-            else:
-                pl.close()
         m.device_error_check()
         best_cfg, best_ms = (plan, t_plan) if t_plan is not None and t_plan < t_model else (cfg_model, t_model)
         sys.stderr.write("%s: model pick %s %.2f us (on a plan: %s), sweep best %s %.2f us\n" % (
             name, tuner.config_name(cfg_model), t_model * 1e3,
             "%.2f us" % (t_plan * 1e3) if t_plan is not None else "n/a", tuner.config_name(cfg_sweep), t_sweep * 1e3))
         results[name] = {"ms": best_ms, "cfg": best_cfg, "model_cfg": cfg_model, "model_ms": t_model,
-                         "plan_ms": t_plan, "plan_sweep": plan_sweep, "tflops": flops / best_ms / 1e9,
+                         "plan_ms": t_plan, "plan_sweep": plan_sweep, "cands": cands, "tflops": flops / best_ms / 1e9,
                          "sweep_ms": t_sweep, "sweep_cfg": cfg_sweep,
                          "err_bar": ERROR_BAR[name], "bytes": algorithmic_bytes(nnzb, cols_touched, name)}
     model.close()
@@ -474,6 +472,13 @@ def run_ours(args, world, rank, local):
     ok = {k: v for k, v in results.items() if v["max_rel"] <= TARGET_ERR} or {"f16": results["f16"]}
     tuned = min(ok, key=lambda k: results[k]["ms"])
     probs, cfg = prepared[tuned], results[tuned]["cfg"]
+    if args.pick_from:
+        # run what an earlier run's line names (its precision and configuration,
+        # among this run's candidates): a profiler's timings must not change the pick
+        prev = json.loads(open(args.pick_from).read().strip().splitlines()[-1])
+        tuned = prev["dtype"]
+        cfg = results[tuned]["cands"][prev["config"]["kernel_config"]]
+        probs = prepared[tuned]
 
     # warm-up, then exactly K timed steps on the tuned configuration
     t_warm = time.time()
@@ -605,8 +610,9 @@ def run_ours(args, world, rank, local):
             "vs_baseline": None, "dtype": tuned, "data": "synthetic (seeded generators)",
             "config": {"workload": WORKLOAD, "precision": tuned,
                        "kernel_config": cfg_name(cfg),
-                       "picked_by": "the learned cost model's pick, or the fastest per-matrix plan over the "
-                                    "tuner's tcgen05 configurations when that is faster",
+                       "picked_by": ("the learned cost model's pick, or the fastest per-matrix plan over the "
+                                     "tuner's tcgen05 configurations when that is faster") if not args.pick_from
+                       else "pinned to the line in %s" % os.path.basename(args.pick_from),
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
                        "nnzb": nnzb,
@@ -742,6 +748,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "f16", "bf16", "e4m3", "f16_split"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pick-from", default=None,
+                    help="run the precision and configuration named by an earlier run's JSON line (for profiling)")
     ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

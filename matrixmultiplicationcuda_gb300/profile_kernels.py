@@ -8,6 +8,9 @@ Families (seeded synthetic inputs; a few hundred MB on the device at most):
   plan_c3   k_bcsr_tc on a per-matrix plan: the same product in bf16 with the
             default tcgen05 configuration (256-column tile, five-group ring,
             two accumulators), items heaviest first from the plan's queue
+  plan_c3_512  the same product in fp16 on a plan with a 512-column tile and
+            one accumulator (one item per CTA), each launch started with
+            SPMM_RUN_INPUTS_READY after the first
   tc_split  k_bcsr_tc in split fp16 (three MMAs per block), same product
   mma_e4m3  k_bcsr_mma: the same product in e4m3 with per-block scales
   mma16     k_bcsr_mma: A 8192^2, 16x16 blocks, random 5 %, N 1024, fp16
@@ -46,7 +49,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="tc,tc_split,mma_e4m3,mma16,batch,convert,quantize,mlp,hybrid,hybrid_plan,csr,"
-                                      "tc64,gen,dense,plan,plan_c3")
+                                      "tc64,gen,dense,plan,plan_c3,plan_c3_512")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args(argv)
     import torch
@@ -158,6 +161,13 @@ def main(argv=None):
         plan = m.BcsrPlan(A, 512)
         run(lambda: plan.run(A, B, C=C))
         print("plan_c3: nnzb=%d, (items, split rows) = %s" % (A.nnzb, plan.info()[:2]))
+        plan.close()
+    if "plan_c3_512" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16)
+        plan = m.BcsrPlan(A, 512, m.Config(kernel=2, n_tile=512, acc_buffers=1))
+        torch.cuda.synchronize()   # no kernel after this writes A or B
+        run(lambda: plan.run(A, B, C=C, inputs_ready=True))
+        print("plan_c3_512: nnzb=%d, (items, split rows) = %s" % (A.nnzb, plan.info()[:2]))
         plan.close()
     if "tc64" in only:
         A, B, Blo, bs, C = c3(m.DType.F16)
