@@ -568,18 +568,33 @@ class Runner {
 
   // Host time per call and back-to-back launch rate (L2 warm: the same buffers
   // every launch; consecutive launches may overlap through programmatic
-  // dependent launch unless SPMM_NO_PDL is set).
-  void launch_bench(const Spec& spec, const char* label) {
+  // dependent launch unless SPMM_NO_PDL is set). plan_nt > 0: the calls are
+  // spmm_bcsr_plan_run_ex on a per-matrix plan with that column tile and one
+  // accumulator, with `flags` (SPMM_RUN_INPUTS_READY: nothing in the loop
+  // writes A or B, so each launch starts while the one before drains C).
+  void launch_bench(const Spec& spec, const char* label, int plan_nt = 0, unsigned flags = 0) {
     DeviceProduct P;
     build_product(spec, P);
     constexpr int kCalls = 200;
-    for (int i = 0; i < 20; ++i) SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, nullptr, nullptr));
+    spmm_bcsr_plan* plan = nullptr;
+    if (plan_nt > 0) {
+      spmm_config pc{};
+      pc.kernel = 2;
+      pc.n_tile = plan_nt;
+      pc.acc_buffers = 1;
+      SK(spmm_bcsr_plan_create(&P.A, P.N, &pc, nullptr, &plan));
+    }
+    auto call = [&] {
+      if (plan) SK(spmm_bcsr_plan_run_ex(plan, &P.A, &P.B, P.N, P.C, P.N, flags, nullptr));
+      else SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, nullptr, nullptr));
+    };
+    for (int i = 0; i < 20; ++i) call();
     CK(cudaDeviceSynchronize());
     double host_us = 1e30, gpu_us = 1e30;
     for (int rep = 0; rep < 5; ++rep) {
       CK(cudaEventRecord(timer_.e0, nullptr));
       const auto t0 = std::chrono::steady_clock::now();
-      for (int i = 0; i < kCalls; ++i) SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, nullptr, nullptr));
+      for (int i = 0; i < kCalls; ++i) call();
       const auto t1 = std::chrono::steady_clock::now();
       CK(cudaEventRecord(timer_.e1, nullptr));
       CK(cudaEventSynchronize(timer_.e1));
@@ -591,6 +606,7 @@ class Runner {
     std::printf("| %s | %s | %.2f us | %.2f us | %.1f |\n", label, std::getenv("SPMM_NO_PDL") ? "off" : "on", host_us,
                 gpu_us, 2.0 * P.nnzb * P.A.bR * 16 * P.N / (gpu_us * 1e-6) / 1e12);
     std::fflush(stdout);
+    if (plan) SK(spmm_bcsr_plan_destroy(plan));
   }
 
   // The same product as BCSR (cost-model configuration), as CSR (the native
@@ -924,11 +940,14 @@ int main(int argc, char** argv) {
     } else if (p == "hybrid") {
       run.hybrid_bench();
     } else if (p == "launch") {
-      std::printf("\n## launch: host time per spmm_bcsr_mm call, back-to-back launches (L2 warm)\n\n");
+      std::printf("\n## launch: host time per call, back-to-back launches (L2 warm)\n\n");
       std::printf("| product | PDL | host per call | GPU per launch | TFLOP/s |\n|---|---|---|---|---|\n");
-      run.launch_bench(Spec{"launch", 1024, 1024, 1024, 16, 4, 0.10, 0.0, 0, 0, SPMM_F16, 123}, "1024^2 16x16 10%, N 1024");
-      run.launch_bench(Spec{"launch", 16384, 16384, 512, 64, 0, 0.02, 0.0, 1, 2, SPMM_F16, 20240},
-                       "16384^2 64x16 2%, N 512");
+      run.launch_bench(Spec{"launch", 1024, 1024, 1024, 16, 4, 0.10, 0.0, 0, 0, SPMM_F16, 123},
+                       "1024^2 16x16 10%, N 1024, spmm_bcsr_mm");
+      const Spec c3{"launch", 16384, 16384, 512, 64, 0, 0.02, 0.0, 1, 2, SPMM_F16, 20240};
+      run.launch_bench(c3, "16384^2 64x16 2%, N 512, spmm_bcsr_mm");
+      run.launch_bench(c3, "the same, plan (512 columns)", 512, 0u);
+      run.launch_bench(c3, "the same, plan (512 columns), SPMM_RUN_INPUTS_READY", 512, SPMM_RUN_INPUTS_READY);
     } else {
       std::fprintf(stderr, "unknown preset %s\n", p.c_str());
       return 1;
