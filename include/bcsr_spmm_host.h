@@ -55,6 +55,16 @@ long long spmm_host_dense_to_bcsr(const void* A_half, int rows, int cols, int bR
 long long spmm_host_dense_to_csr(const void* A_half, int rows, int cols, int* hdr, int* idx,
                                  void* vals);
 
+/* The per-matrix plan's item list (spmm_bcsr_plan_create, bcsr_spmm.h) on
+ * the host, for row_ptr (MB + 1 entries), `ntiles` column tiles and `slots`
+ * CTA slots (SMs x CTAs per SM): rows longer than 3x the average load per
+ * slot cut into parts, items ordered heaviest first (the parts of a row
+ * together, part 0 first). items: 4 ints per item {block row, column tile,
+ * first block, end block}; pair: -1, or 128 * group + part; parts: parts per
+ * group. Pass NULL arrays to get *n_items and *n_groups first. */
+spmm_status spmm_bcsr_plan_items(const int* row_ptr, int MB, int ntiles, long long slots, int* n_items,
+                                 int* n_groups, int* items, int* pair, int* parts);
+
 /* Matrix Market files (.mtx): what the reference's generator writes through
  * scipy's mmwrite (matrix_generator.py:100-108). Coordinate (real, integer or
  * pattern; general, symmetric or skew-symmetric) and array (real, general)

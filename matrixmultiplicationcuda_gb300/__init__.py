@@ -50,6 +50,7 @@ from .bcsr import (  # noqa: F401
 from .host import (  # noqa: F401
     generate_matrix,
     gen_structure,
+    plan_items,
     gen_values,
     gen_dense,
     host_dense_to_bcsr,

@@ -46,6 +46,47 @@ constexpr int kMinPartBlocks = 8;   // shorter parts are not worth a hand-off
 constexpr int kSplitFactor = 3;     // split rows longer than 3x the average load per CTA slot
 constexpr int kMaxParts = 64;
 
+struct Item {
+  int4 d;    // {block row, column tile, first block, end block}
+  int pair;  // -1, or 128 * group + part
+  int key;   // heaviness: its blocks, or for a part the longest part of its row
+};
+
+// The item list for row_ptr (MB + 1 entries), ntiles column tiles and
+// `capacity` CTA slots: rows far above the average load per slot cut into
+// parts, every item keyed by its heaviness, sorted heaviest first. Host code
+// only; the device plan and spmm_bcsr_plan_items both use it.
+void build_items(const int* rp, int MB, int ntiles, long long capacity, std::vector<Item>* out,
+                 std::vector<int>* group_parts) {
+  std::vector<Item>& items = *out;
+  items.clear();
+  group_parts->clear();
+  long long total = 0;
+  for (int r = 0; r < MB; ++r) total += (long long)(rp[r + 1] - rp[r]) * ntiles;
+  const long long avg = std::max<long long>(kMinPartBlocks, (total + capacity - 1) / capacity);
+  items.reserve((size_t)MB * ntiles + 64);
+  for (int r = 0; r < MB; ++r) {
+    const int len = rp[r + 1] - rp[r];
+    const int k = len > kSplitFactor * avg ? (int)std::min<long long>(kMaxParts, (len + avg - 1) / avg) : 1;
+    for (int t = 0; t < ntiles; ++t) {
+      if (k == 1) {
+        items.push_back({make_int4(r, t, rp[r], rp[r + 1]), -1, len});
+        continue;
+      }
+      const int g = (int)group_parts->size();
+      group_parts->push_back(k);
+      for (int q = 0; q < k; ++q)
+        items.push_back({make_int4(r, t, rp[r] + (int)((long long)len * q / k), rp[r] + (int)((long long)len * (q + 1) / k)),
+                         128 * g + q, (len + k - 1) / k});
+    }
+  }
+  // Heaviest first: with more items than CTAs, each CTA's next item is lighter.
+  // The parts of a row share one key, so the stable sort keeps part 0 ahead of
+  // its siblings: a CTA takes its items in list order, so every part waits only
+  // for a part 0 earlier in the list, and those waits cannot form a cycle.
+  std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.key > b.key; });
+}
+
 void plan_free(spmm_bcsr_plan* p) {
   if (!p) return;
   cudaFree(p->items);
@@ -91,42 +132,12 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   for (int r = 0; r < MB; ++r)
     if (rp[r + 1] < rp[r]) return fail(SPMM_ERR_INVALID_ARG, "row_ptr must not decrease");
   const int ntiles = (N + nt - 1) / nt;
-  const long long base = (long long)MB * ntiles;
   const long long capacity = (long long)sm_count() * per_sm;
-  // the average load per CTA slot, and the rows far above it
-  long long total = 0;
-  for (int r = 0; r < MB; ++r) total += (long long)(rp[r + 1] - rp[r]) * ntiles;
-  const long long avg = std::max<long long>(kMinPartBlocks, (total + capacity - 1) / capacity);
-  struct Item {
-    int4 d;
-    int pair;
-    int key;   // heaviness: its blocks, or for a part the longest part of its row
-  };
   std::vector<Item> items;
   std::vector<int> group_parts;
-  items.reserve((size_t)base + 64);
-  for (int r = 0; r < MB; ++r) {
-    const int len = rp[r + 1] - rp[r];
-    const int k = len > kSplitFactor * avg ? (int)std::min<long long>(kMaxParts, (len + avg - 1) / avg) : 1;
-    for (int t = 0; t < ntiles; ++t) {
-      if (k == 1) {
-        items.push_back({make_int4(r, t, rp[r], rp[r + 1]), -1, len});
-        continue;
-      }
-      const int g = (int)group_parts.size();
-      group_parts.push_back(k);
-      for (int q = 0; q < k; ++q)
-        items.push_back({make_int4(r, t, rp[r] + (int)((long long)len * q / k), rp[r] + (int)((long long)len * (q + 1) / k)),
-                         128 * g + q, (len + k - 1) / k});
-    }
-  }
+  build_items(rp.data(), MB, ntiles, capacity, &items, &group_parts);
   const int pairs = (int)group_parts.size();
   if (items.size() >= (1u << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
-  // Heaviest first: with more items than CTAs, each CTA's next item is lighter.
-  // The parts of a row share one key, so the stable sort keeps part 0 ahead of
-  // its siblings: a CTA takes its items in list order, so every part waits only
-  // for a part 0 earlier in the list, and those waits cannot form a cycle.
-  std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.key > b.key; });
   std::vector<int4> hd(items.size());
   std::vector<int> hp(items.size());
   for (size_t i = 0; i < items.size(); ++i) {
@@ -207,5 +218,31 @@ extern "C" spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* p, const spmm
 
 extern "C" spmm_status spmm_bcsr_plan_destroy(spmm_bcsr_plan* p) {
   plan_free(p);
+  return SPMM_OK;
+}
+
+extern "C" spmm_status spmm_bcsr_plan_items(const int* row_ptr, int MB, int ntiles, long long slots, int* n_items,
+                                            int* n_groups, int* items, int* pair, int* parts) {
+  if (!row_ptr || MB < 0 || ntiles < 1 || slots < 1 || !n_items || !n_groups)
+    return fail(SPMM_ERR_INVALID_ARG, "bad plan-items arguments");
+  for (int r = 0; r < MB; ++r)
+    if (row_ptr[r + 1] < row_ptr[r]) return fail(SPMM_ERR_INVALID_ARG, "row_ptr must not decrease");
+  std::vector<Item> list;
+  std::vector<int> group_parts;
+  build_items(row_ptr, MB, ntiles, slots, &list, &group_parts);
+  if (list.size() >= (1u << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
+  *n_items = (int)list.size();
+  *n_groups = (int)group_parts.size();
+  for (size_t i = 0; i < list.size(); ++i) {
+    if (items) {
+      items[4 * i] = list[i].d.x;
+      items[4 * i + 1] = list[i].d.y;
+      items[4 * i + 2] = list[i].d.z;
+      items[4 * i + 3] = list[i].d.w;
+    }
+    if (pair) pair[i] = list[i].pair;
+  }
+  if (parts)
+    for (size_t g = 0; g < group_parts.size(); ++g) parts[g] = group_parts[g];
   return SPMM_OK;
 }

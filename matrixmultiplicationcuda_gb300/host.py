@@ -35,6 +35,22 @@ def gen_structure(M, K, bR, pattern, density, param=0.0, seed=1):
     return rp, ci[:n].copy()
 
 
+def plan_items(row_ptr, ntiles, slots):
+    """The per-matrix plan's item list on the host (spmm_bcsr_plan_items):
+    (items [n, 4] = {block row, column tile, first block, end block} heaviest
+    first, pair [n] = -1 or 128 * group + part, parts [groups])."""
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    n, g = ctypes.c_int(), ctypes.c_int()
+    check(lib().spmm_bcsr_plan_items(_vp(rp), len(rp) - 1, int(ntiles), int(slots), ctypes.byref(n), ctypes.byref(g),
+                                     None, None, None))
+    items = np.empty((max(n.value, 1), 4), np.int32)
+    pair = np.empty(max(n.value, 1), np.int32)
+    parts = np.empty(max(g.value, 1), np.int32)
+    check(lib().spmm_bcsr_plan_items(_vp(rp), len(rp) - 1, int(ntiles), int(slots), ctypes.byref(n), ctypes.byref(g),
+                                     _vp(items), _vp(pair), _vp(parts)))
+    return items[:n.value], pair[:n.value], parts[:g.value]
+
+
 def gen_values(nnzb, bR, bC=16, dist=DIST_UNIFORM, seed=2):
     out = np.empty(nnzb * bR * bC, np.float32)
     lib().spmm_gen_values(nnzb, bR, bC, dist, seed, _vp(out))
