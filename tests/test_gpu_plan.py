@@ -255,3 +255,41 @@ def test_plan_run_rejects_unknown_flags(dev):
                                      256, 2, stream_handle(None))
     assert st == int(m.Status.INVALID_ARG)
     plan.close()
+
+
+def test_plan_inputs_ready_in_cuda_graph(dev):
+    """A chain of flagged plan runs over four independent products, captured in
+    one CUDA graph (consecutive launches keep their programmatic dependency)
+    and replayed: every C matches the eager product bit for bit."""
+    M = K = 8192
+    N = 512
+    probs = []
+    for s in range(4):
+        A, B = _int_problem(M, K, N, 64, m.PATTERN_LOGNORMAL, 0.05, 40 + s, dev)
+        probs.append((A, B))
+    plans = [m.BcsrPlan(A, N, m.Config(kernel=2, n_tile=512, acc_buffers=1)) for A, _ in probs]
+    refs = [p.run(A, B).clone() for p, (A, B) in zip(plans, probs)]
+    Cs = [torch.empty((M, N), dtype=torch.float32, device=dev) for _ in probs]
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for p, (A, B), C in zip(plans, probs, Cs):
+            p.run(A, B, C=C, stream=s, inputs_ready=True)   # warm-up on the capture stream
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        st = torch.cuda.current_stream()
+        for p, (A, B), C in zip(plans, probs, Cs):
+            p.run(A, B, C=C, stream=st, inputs_ready=True)
+    for _ in range(3):
+        for C in Cs:
+            C.fill_(float("nan"))
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        m.device_error_check()
+        for C, ref in zip(Cs, refs):
+            assert torch.equal(C, ref)
+    for p in plans:
+        p.close()
