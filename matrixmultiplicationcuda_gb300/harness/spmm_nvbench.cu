@@ -39,6 +39,10 @@
 //       BCSR pipeline with every block stored, the native dense GEMM, and
 //       cuBLAS GemmEx.
 //   hybrid  the hybrid BCSR + CSR product across density thresholds.
+//
+// Tunings: default (the library's choice), model (the cost model's pick),
+// plan (a per-matrix plan on each tcgen05 configuration of the tuner's table
+// without split-K, the fastest reported), sweep (the exhaustive sweep's best).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
@@ -449,26 +453,32 @@ class Runner {
       r.spec = spec;
       r.tuning = tuning;
       if (tuning == "plan") {
-        // the per-matrix plan on the tcgen05 pipeline: the model's configuration
-        // when it runs there (without split-K; the plan brings its own work
-        // queue), else its default
-        spmm_config mc{};
-        if (model_) SK(spmm_cost_model_select(model_, &P.A, P.N, &mc, nullptr, nullptr));
-        if (mc.kernel == 2) {
-          mc.split_k = 0;
-          mc.schedule = 0;
-        } else {
-          std::memset(&mc, 0, sizeof(mc));
-          mc.kernel = 2;
+        // a per-matrix plan on each tcgen05 configuration of the tuner's table
+        // without split-K (the plan brings its own work queue), each timed the
+        // same way; the row is the fastest, and its product is the one checked
+        spmm_bcsr_plan* best = nullptr;
+        for (int i = 0; i < spmm_tune_config_count(); ++i) {
+          spmm_config tc{};
+          SK(spmm_tune_config(i, &tc));
+          if (tc.kernel != 2 || tc.split_k > 1 || tc.schedule != 0) continue;
+          spmm_bcsr_plan* plan = nullptr;
+          if (spmm_bcsr_plan_create(&P.A, P.N, &tc, nullptr, &plan) != SPMM_OK) continue;   // no kernel for it
+          const Sample smp = timer_.measure([&] { SK(spmm_bcsr_plan_run(plan, &P.A, &P.B, P.N, P.C, P.N, nullptr)); }, o_);
+          if (!best || smp.mean_us < r.s.mean_us) {
+            if (best) SK(spmm_bcsr_plan_destroy(best));
+            best = plan;
+            r.s = smp;
+          } else {
+            SK(spmm_bcsr_plan_destroy(plan));
+          }
         }
-        spmm_bcsr_plan* plan = nullptr;
-        if (spmm_bcsr_plan_create(&P.A, P.N, &mc, nullptr, &plan) != SPMM_OK) continue;   // no tcgen05 kernel
+        if (!best) continue;   // no tcgen05 kernel for this block height and type
         int items = 0, groups = 0;
         spmm_config pcfg{};
-        SK(spmm_bcsr_plan_info(plan, &items, &groups, &pcfg));
+        SK(spmm_bcsr_plan_info(best, &items, &groups, &pcfg));
         r.config = "plan " + config_name(&pcfg) + " (" + std::to_string(groups) + " rows split)";
-        r.s = timer_.measure([&] { SK(spmm_bcsr_plan_run(plan, &P.A, &P.B, P.N, P.C, P.N, nullptr)); }, o_);
-        SK(spmm_bcsr_plan_destroy(plan));
+        SK(spmm_bcsr_plan_run(best, &P.A, &P.B, P.N, P.C, P.N, nullptr));
+        SK(spmm_bcsr_plan_destroy(best));
       } else {
         r.config = config_name(pc);
         r.s = timer_.measure([&] { SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, pc, nullptr)); }, o_);
