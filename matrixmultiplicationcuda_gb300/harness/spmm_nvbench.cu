@@ -579,10 +579,10 @@ class Runner {
   // Host time per call and back-to-back launch rate (L2 warm: the same buffers
   // every launch; consecutive launches may overlap through programmatic
   // dependent launch unless SPMM_NO_PDL is set). plan_nt > 0: the calls are
-  // spmm_bcsr_plan_run_ex on a per-matrix plan with that column tile and one
-  // accumulator, with `flags` (SPMM_RUN_INPUTS_READY: nothing in the loop
-  // writes A or B, so each launch starts while the one before drains C).
-  void launch_bench(const Spec& spec, const char* label, int plan_nt = 0, unsigned flags = 0) {
+  // spmm_bcsr_plan_run_ex on a per-matrix plan with that column tile and
+  // `plan_acc` accumulators, with `flags` (SPMM_RUN_INPUTS_READY: nothing in
+  // the loop writes A or B, so each launch starts while the one before drains C).
+  void launch_bench(const Spec& spec, const char* label, int plan_nt = 0, unsigned flags = 0, int plan_acc = 1) {
     DeviceProduct P;
     build_product(spec, P);
     constexpr int kCalls = 200;
@@ -591,7 +591,7 @@ class Runner {
       spmm_config pc{};
       pc.kernel = 2;
       pc.n_tile = plan_nt;
-      pc.acc_buffers = 1;
+      pc.acc_buffers = plan_acc;
       SK(spmm_bcsr_plan_create(&P.A, P.N, &pc, nullptr, &plan));
     }
     auto call = [&] {
@@ -952,8 +952,10 @@ int main(int argc, char** argv) {
     } else if (p == "launch") {
       std::printf("\n## launch: host time per call, back-to-back launches (L2 warm)\n\n");
       std::printf("| product | PDL | host per call | GPU per launch | TFLOP/s |\n|---|---|---|---|---|\n");
-      run.launch_bench(Spec{"launch", 1024, 1024, 1024, 16, 4, 0.10, 0.0, 0, 0, SPMM_F16, 123},
-                       "1024^2 16x16 10%, N 1024, spmm_bcsr_mm");
+      const Spec c1{"launch", 1024, 1024, 1024, 16, 4, 0.10, 0.0, 0, 0, SPMM_F16, 123};
+      run.launch_bench(c1, "1024^2 16x16 10%, N 1024, spmm_bcsr_mm");
+      run.launch_bench(c1, "the same, plan (256 columns)", 256, 0u, 2);
+      run.launch_bench(c1, "the same, plan (256 columns), SPMM_RUN_INPUTS_READY", 256, SPMM_RUN_INPUTS_READY, 2);
       const Spec c3{"launch", 16384, 16384, 512, 64, 0, 0.02, 0.0, 1, 2, SPMM_F16, 20240};
       run.launch_bench(c3, "16384^2 64x16 2%, N 512, spmm_bcsr_mm");
       run.launch_bench(c3, "the same, plan (512 columns)", 512, 0u);
