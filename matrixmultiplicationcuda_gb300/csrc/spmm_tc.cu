@@ -850,9 +850,9 @@ spmm_status launch_tc(const LaunchRequest& r) {
   if (std::getenv("SPMM_DEBUG"))
     std::fprintf(stderr,
                  "[spmm] tcgen05 bR=%d nt=%d stages=%d acc=%d group=%d smem=%zu tmem=%d per_sm=%d grid=%lld "
-                 "items=%d panel3d=%d queue=%d split=%d\n",
+                 "items=%d panel3d=%d queue=%d claim_ahead=%d inputs_ready=%d split=%d\n",
                  A.bR, nt, e->stages, e->acc, e->group, e->smem, e->tmem_cols, per_sm, grid, p.n_items, panel3d,
-                 p.queue != nullptr, p.split);
+                 p.queue != nullptr, p.claim_ahead, p.inputs_ready, p.split);
   SPMM_CUDA_TRY(launch_kernel(e->fn, dim3((unsigned)grid), dim3(kTcThreads), e->smem, r.stream, tmA1, tmAg, tmAlo1,
                               tmAlog, tmB, tmBlo, p));
   return SPMM_OK;
