@@ -347,8 +347,20 @@ spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr
  * at a time (its queue and counters are its own; use one plan per stream for
  * concurrent launches). cfg: kernel 0 or 2, no split-K, schedule 0 or 1
  * (either way the plan's own queue; _info reports schedule 1).
+ * 16- and 32-row blocks (fp16 / bf16, M a multiple of 64): when the 4 (or 2)
+ *   block rows that make up 64 rows of C share most of their block columns
+ *   (the union holds at most 60 % of their blocks, as in band and
+ *   block-diagonal structures), the plan stacks them into 64-row blocks with
+ *   zeros where a row has no block, and a run first copies A's values into
+ *   them (one small kernel) and then runs the 64-row pipeline: one UMMA and
+ *   one B panel for up to 4 blocks. A stacked plan is built from col_idx as
+ *   well, so A's column indices must stay the plan's; it runs without the
+ *   early start of SPMM_RUN_INPUTS_READY (its pipeline reads the copy made
+ *   just before).
  * spmm_bcsr_plan_info: item count, split rows (row and column-tile pairs),
- * and the configuration the plan runs. */
+ * and the configuration the plan runs (for a stacked plan, the 64-row one).
+ * spmm_bcsr_plan_stacking: block rows per stacked row (1: not stacked) and
+ * the stacked blocks. */
 typedef struct spmm_bcsr_plan spmm_bcsr_plan;
 spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, const spmm_config* cfg, void* stream,
                                   spmm_bcsr_plan** plan_out);
@@ -367,6 +379,7 @@ spmm_status spmm_bcsr_plan_run(const spmm_bcsr_plan* plan, const spmm_bcsr_desc*
 #define SPMM_RUN_INPUTS_READY 1u
 spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* plan, const spmm_bcsr_desc* A, const spmm_dense_desc* B,
                                   int N, float* C, int ldc, unsigned flags, void* stream);
+spmm_status spmm_bcsr_plan_stacking(const spmm_bcsr_plan* plan, int* rows_per_stack, long long* stacked_blocks);
 spmm_status spmm_bcsr_plan_destroy(spmm_bcsr_plan* plan);
 
 /* ---- allocation-free variant ---------------------------------------------------

@@ -90,6 +90,7 @@ _SIGS = {
                                    c_vp]),
     "spmm_bcsr_plan_run_ex": (c_int, [c_vp, ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp, c_int,
                                       ctypes.c_uint, c_vp]),
+    "spmm_bcsr_plan_stacking": (c_int, [c_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_ll)]),
     "spmm_bcsr_plan_destroy": (c_int, [c_vp]),
     "spmm_dense_mm": (c_int, [c_vp, c_int, ctypes.POINTER(DenseDesc), c_int, c_int, c_int, c_int, c_vp, c_int,
                               c_vp]),

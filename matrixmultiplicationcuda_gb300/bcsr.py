@@ -147,6 +147,13 @@ class BcsrPlan:
         check(lib().spmm_bcsr_plan_info(self._h, ctypes.byref(n), ctypes.byref(sp), ctypes.byref(c)))
         return n.value, sp.value, c
 
+    def stacking(self):
+        """(block rows per stacked 64-row row, stacked blocks); (1, 0) when the
+        plan runs the blocks as they are."""
+        st, nb = ctypes.c_int(), ctypes.c_longlong()
+        check(lib().spmm_bcsr_plan_stacking(self._h, ctypes.byref(st), ctypes.byref(nb)))
+        return st.value, nb.value
+
     def run(self, A: BCSR, B, C=None, stream=None, B_lo=None, b_scale=1.0, ldc=None, inputs_ready=False):
         """One launch. inputs_ready=True (SPMM_RUN_INPUTS_READY) promises that no
         kernel launched on the stream since its last host synchronisation writes A

@@ -18,8 +18,20 @@
 // items at the end of the list. Claims follow list order, and so does each
 // CTA's own sequence of items.
 //
-// The plan holds only what row_ptr determines: any A with the same M, K, block
-// shape, dtype and row_ptr (values and column indices may change) runs on it.
+// Stacking (16- and 32-row blocks): the tcgen05 UMMA costs the same for a
+// block height of 16, 32 or 64, and every block loads its own B panel. When
+// the 4 (or 2) block rows that make up 64 rows of C share most of their block
+// columns (band and block-diagonal structures), the plan stacks them: the
+// union of their columns becomes one 64-row BCSR row whose blocks hold the
+// member rows' blocks and zeros, so one UMMA and one B panel serve 4 (or 2)
+// blocks. A run copies the current values into the stacked blocks (one small
+// kernel) and runs the 64-row pipeline. The plan stacks only when the union
+// saves at least 40 % of the panels.
+//
+// The plan holds only what row_ptr (and, for a stacked plan, col_idx)
+// determines: any A with the same M, K, block shape, dtype and structure
+// (values may change; column indices too for a plan that does not stack) runs
+// on it.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -37,6 +49,13 @@ struct spmm_bcsr_plan {
   int* parts = nullptr;        // parts per group (split row and tile)
   unsigned* counters = nullptr;   // per group: {C tile zeroed, parts finished}; then the queue
   unsigned* queue = nullptr;      // {next ticket, CTAs done}, inside `counters`
+  // stacking: `stack` block rows per 64-row row (1: none)
+  int stack = 1;
+  long long stacked_blocks = 0;
+  int* s_row_ptr = nullptr;       // M/64 + 1
+  int* s_col_idx = nullptr;       // stacked_blocks
+  int* s_map = nullptr;           // stacked_blocks x stack: source block of each member row, or -1
+  void* s_vals = nullptr;         // stacked_blocks x 64 x 16 values, refilled by every run
 };
 
 namespace spmm {
@@ -45,6 +64,61 @@ namespace {
 constexpr int kMinPartBlocks = 8;   // shorter parts are not worth a hand-off
 constexpr int kSplitFactor = 3;     // split rows longer than 3x the average load per CTA slot
 constexpr int kMaxParts = 64;
+constexpr int kStackKeepPct = 60;   // stack when the union has at most 60 % of the blocks
+
+// One thread per 16-byte chunk of a member block in the stacked layout: chunk
+// x of member i (= stacked block * stack + member row) is chunk x of source
+// block map[i], or zeros.
+__global__ void k_stack_repack(const int4* __restrict__ src, const int* __restrict__ map, long long members,
+                               int chunks, int4* __restrict__ dst) {
+  const long long n = members * chunks;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    const long long i = x / chunks;
+    const int b = __ldg(map + i);
+    dst[x] = b >= 0 ? __ldg(src + (long long)b * chunks + (x - i * chunks)) : make_int4(0, 0, 0, 0);
+  }
+}
+
+// The stacked structure of 16- or 32-row blocks: for each group of `st` block
+// rows (64 rows of C), the sorted union of their block columns, and per union
+// column the block of each member row (or -1). False when a row repeats a
+// column (the stacked block could not hold both).
+bool build_stack(const int* rp, const int* ci, int MB, int st, std::vector<int>* srp, std::vector<int>* sci,
+                 std::vector<int>* smap) {
+  const int MS = MB / st;
+  srp->assign(1, 0);
+  sci->clear();
+  smap->clear();
+  std::vector<std::pair<int, int>> ent;   // (column, entry) of the group's blocks
+  std::vector<int> member, block;         // per entry: member row, source block
+  for (int g = 0; g < MS; ++g) {
+    ent.clear();
+    member.clear();
+    block.clear();
+    for (int t = 0; t < st; ++t) {
+      const int r = g * st + t;
+      for (int b = rp[r]; b < rp[r + 1]; ++b) {
+        ent.push_back({ci[b], (int)member.size()});
+        member.push_back(t);
+        block.push_back(b);
+      }
+    }
+    std::sort(ent.begin(), ent.end());
+    for (size_t i = 0; i < ent.size();) {
+      const int c = ent[i].first;
+      const size_t base = smap->size();
+      smap->resize(base + st, -1);
+      for (; i < ent.size() && ent[i].first == c; ++i) {
+        const int k = ent[i].second;
+        if ((*smap)[base + member[k]] >= 0) return false;   // a row repeats a column
+        (*smap)[base + member[k]] = block[k];
+      }
+      sci->push_back(c);
+    }
+    srp->push_back((int)sci->size());
+  }
+  return true;
+}
 
 struct Item {
   int4 d;    // {block row, column tile, first block, end block}
@@ -93,6 +167,10 @@ void plan_free(spmm_bcsr_plan* p) {
   cudaFree(p->pair);
   cudaFree(p->parts);
   cudaFree(p->counters);
+  cudaFree(p->s_row_ptr);
+  cudaFree(p->s_col_idx);
+  cudaFree(p->s_map);
+  cudaFree(p->s_vals);
   delete p;
 }
 
@@ -120,10 +198,6 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
     return fail(SPMM_ERR_UNSUPPORTED, "a plan replaces split-K and brings its own work queue");
   c.kernel = 2;
   c.schedule = 1;   // the plan's queue
-  int nt = 0, per_sm = 0;
-  if (!tc_geometry(A->bR, A->dtype, N, c, &nt, &per_sm))
-    return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for this block height, dtype and configuration");
-  c.n_tile = nt;
   const int MB = A->M / A->bR;
   std::vector<int> rp(MB + 1);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -131,11 +205,29 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   SPMM_CUDA_TRY(cudaStreamSynchronize(s));
   for (int r = 0; r < MB; ++r)
     if (rp[r + 1] < rp[r]) return fail(SPMM_ERR_INVALID_ARG, "row_ptr must not decrease");
+  // stacking of 16- and 32-row blocks into the 64-row pipeline
+  int st = 1, nt = 0, per_sm = 0;
+  std::vector<int> srp, sci, smap;
+  const long long nnzb = rp[MB];
+  if ((A->bR == 16 || A->bR == 32) && A->M % 64 == 0 && (A->dtype == SPMM_F16 || A->dtype == SPMM_BF16) &&
+      nnzb > 0 && A->col_idx && A->vals && tc_geometry(64, A->dtype, N, c, &nt, &per_sm)) {
+    std::vector<int> ci((size_t)nnzb);
+    SPMM_CUDA_TRY(cudaMemcpyAsync(ci.data(), A->col_idx, sizeof(int) * nnzb, cudaMemcpyDeviceToHost, s));
+    SPMM_CUDA_TRY(cudaStreamSynchronize(s));
+    const int cand = 64 / A->bR;
+    if (build_stack(rp.data(), ci.data(), MB, cand, &srp, &sci, &smap) &&
+        (long long)sci.size() * 100 <= nnzb * kStackKeepPct)
+      st = cand;
+  }
+  if (st == 1 && !tc_geometry(A->bR, A->dtype, N, c, &nt, &per_sm))
+    return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for this block height, dtype and configuration");
+  c.n_tile = nt;
+  const int rows = st > 1 ? A->M / 64 : MB;
   const int ntiles = (N + nt - 1) / nt;
   const long long capacity = (long long)sm_count() * per_sm;
   std::vector<Item> items;
   std::vector<int> group_parts;
-  build_items(rp.data(), MB, ntiles, capacity, &items, &group_parts);
+  build_items(st > 1 ? srp.data() : rp.data(), rows, ntiles, capacity, &items, &group_parts);
   const int pairs = (int)group_parts.size();
   if (items.size() >= (1u << 30)) return fail(SPMM_ERR_UNSUPPORTED, "too many work items");
   std::vector<int4> hd(items.size());
@@ -168,7 +260,32 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
     return fail(SPMM_ERR_CUDA, "plan upload failed");
   }
   p->queue = p->counters + 2 * std::max(pairs, 1);
+  if (st > 1) {
+    // the stacked structure, and room for the stacked values every run refills
+    p->stack = st;
+    p->stacked_blocks = (long long)sci.size();
+    if (cudaMalloc(&p->s_row_ptr, sizeof(int) * srp.size()) != cudaSuccess ||
+        cudaMalloc(&p->s_col_idx, sizeof(int) * sci.size()) != cudaSuccess ||
+        cudaMalloc(&p->s_map, sizeof(int) * smap.size()) != cudaSuccess ||
+        cudaMalloc(&p->s_vals, (size_t)p->stacked_blocks * 64 * 16 * 2) != cudaSuccess) {
+      plan_free(p);
+      return fail(SPMM_ERR_CUDA, "stacked plan allocation failed");
+    }
+    if (cudaMemcpy(p->s_row_ptr, srp.data(), sizeof(int) * srp.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(p->s_col_idx, sci.data(), sizeof(int) * sci.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(p->s_map, smap.data(), sizeof(int) * smap.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      plan_free(p);
+      return fail(SPMM_ERR_CUDA, "stacked plan upload failed");
+    }
+  }
   *out = p;
+  return SPMM_OK;
+}
+
+extern "C" spmm_status spmm_bcsr_plan_stacking(const spmm_bcsr_plan* p, int* rows_per_stack, long long* blocks) {
+  if (!p) return fail(SPMM_ERR_INVALID_ARG, "null plan");
+  if (rows_per_stack) *rows_per_stack = p->stack;
+  if (blocks) *blocks = p->stacked_blocks;
   return SPMM_OK;
 }
 
@@ -198,21 +315,43 @@ extern "C" spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* p, const spmm
   auto al16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
   if ((A->vals && !al16(A->vals)) || !al16(B->data) || !al16(C))
     return fail(SPMM_ERR_MISALIGNED, "A values, B and C must be 16-byte aligned");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  spmm_bcsr_desc a64;
+  const spmm_bcsr_desc* Arun = A;
+  if (p->stack > 1) {
+    // this run's values into the stacked 64-row blocks; the pipeline then
+    // reads them, so it waits for this kernel (no early start)
+    if (!A->vals) return fail(SPMM_ERR_INVALID_ARG, "null values");
+    const int chunks = p->bR * 2;   // 16-byte chunks of a bR x 16 block of 2-byte values
+    const long long n = p->stacked_blocks * p->stack * chunks;
+    const long long grid = std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
+    k_stack_repack<<<(unsigned)grid, 256, 0, s>>>(static_cast<const int4*>(A->vals), p->s_map,
+                                                  p->stacked_blocks * p->stack, chunks, static_cast<int4*>(p->s_vals));
+    SPMM_CUDA_TRY(cudaGetLastError());
+    a64 = *A;
+    a64.bR = 64;
+    a64.row_ptr = p->s_row_ptr;
+    a64.col_idx = p->s_col_idx;
+    a64.vals = p->s_vals;
+    a64.vals_lo = nullptr;
+    a64.scales = nullptr;
+    Arun = &a64;
+  }
   LaunchRequest r;
-  r.A = A;
+  r.A = Arun;
   r.B = B;
   r.N = N;
   r.C = C;
   r.ldc = ldc;
   r.cfg = p->cfg;
-  r.stream = static_cast<cudaStream_t>(stream);
+  r.stream = s;
   r.items = p->items;
   r.pair = p->n_pairs > 0 ? p->pair : nullptr;
   r.parts = p->parts;
   r.counters = p->counters;
   r.plan_items = p->n_items;
   r.queue = p->queue;
-  r.inputs_ready = (flags & SPMM_RUN_INPUTS_READY) != 0;
+  r.inputs_ready = (flags & SPMM_RUN_INPUTS_READY) != 0 && p->stack == 1;
   return launch_tc(r);
 }
 

@@ -293,3 +293,79 @@ def test_plan_inputs_ready_in_cuda_graph(dev):
             assert torch.equal(C, ref)
     for p in plans:
         p.close()
+
+
+def _int_bcsr(M, K, bR, pattern, density, param, seed, dev, dtype=m.DType.F16):
+    rp, ci = m.gen_structure(M, K, bR, pattern, density, param, seed=seed)
+    rng = np.random.default_rng(seed)
+    vals = rng.integers(-2, 3, len(ci) * bR * 16).astype(np.float32)
+    return rp, ci, vals, m.BCSR.from_host(M, K, bR, rp, ci, vals, dtype, device=dev)
+
+
+@pytest.mark.parametrize("bR", [16, 32])
+@pytest.mark.parametrize("pattern,param", [(m.PATTERN_BAND, 8), (m.PATTERN_BLOCKDIAG, 256)])
+@pytest.mark.parametrize("N,cfg", [(512, None), (264, m.Config(kernel=2, n_tile=512, acc_buffers=1))])
+def test_plan_stacks_short_blocks(dev, bR, pattern, param, N, cfg):
+    """16- and 32-row blocks whose block rows share their columns (band,
+    block-diagonal) run stacked as 64-row blocks: the same product as the
+    unplanned one, exactly (integer inputs), and new values on the same
+    structure are picked up by the next run."""
+    M = K = 4096
+    rp, ci, vals, A = _int_bcsr(M, K, bR, pattern, 0.2, param, 11, dev)
+    B = torch.from_numpy(np.random.default_rng(12).integers(-2, 3, (K, N)).astype(np.float32)).to(dev).half()
+    plan = m.BcsrPlan(A, N, cfg)
+    st, nb = plan.stacking()
+    assert st == 64 // bR and 0 < nb * 100 <= len(ci) * 60
+    ref = m.spmm(A, B, N=N)
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    plan.run(A, B, C=C)
+    m.device_error_check()
+    assert torch.equal(C, ref)
+    A2 = m.BCSR.from_host(M, K, bR, rp, ci, -2 * vals, m.DType.F16, device=dev)   # same structure
+    torch.cuda.synchronize()
+    plan.run(A2, B, C=C, inputs_ready=True)   # a stacked plan runs without the early start
+    m.device_error_check()
+    assert torch.equal(C, -2 * ref)
+    plan.close()
+
+
+@pytest.mark.parametrize("M,pattern,density", [(4096, m.PATTERN_RANDOM, 0.05),        # columns rarely shared
+                                               (4096 + 16, m.PATTERN_BAND, 0.2)])     # M not a multiple of 64
+def test_plan_does_not_stack(dev, M, pattern, density):
+    K, N = 4096, 256
+    rp, ci, vals, A = _int_bcsr(M, K, 16, pattern, density, 8, 13, dev)
+    B = torch.from_numpy(np.random.default_rng(14).integers(-2, 3, (K, N)).astype(np.float32)).to(dev).half()
+    plan = m.BcsrPlan(A, N)
+    assert plan.stacking() == (1, 0)
+    assert torch.equal(plan.run(A, B), m.spmm(A, B, N=N))
+    m.device_error_check()
+    plan.close()
+
+
+def test_plan_stacked_bf16_in_cuda_graph(dev):
+    """A stacked run is two launches (the copy into 64-row blocks, then the
+    pipeline); captured in a graph and replayed it matches the eager product."""
+    M = K = 8192
+    N = 512
+    rp, ci, vals, A = _int_bcsr(M, K, 16, m.PATTERN_BAND, 0.2, 8, 15, dev, m.DType.BF16)
+    B = torch.from_numpy(np.random.default_rng(16).integers(-2, 3, (K, N)).astype(np.float32)).to(dev).bfloat16()
+    plan = m.BcsrPlan(A, N)
+    assert plan.stacking()[0] == 4
+    eager = m.spmm(A, B, N=N)
+    C = torch.empty((M, N), dtype=torch.float32, device=dev)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.run(A, B, C=C, stream=s)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.run(A, B, C=C, stream=torch.cuda.current_stream())
+    for _ in range(3):
+        C.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        m.device_error_check()
+        assert torch.equal(C, eager)
+    plan.close()
