@@ -304,7 +304,7 @@ def _int_bcsr(M, K, bR, pattern, density, param, seed, dev, dtype=m.DType.F16):
 
 @pytest.mark.parametrize("bR", [16, 32])
 @pytest.mark.parametrize("pattern,param", [(m.PATTERN_BAND, 8), (m.PATTERN_BLOCKDIAG, 256)])
-@pytest.mark.parametrize("N,cfg", [(512, None), (264, m.Config(kernel=2, n_tile=512, acc_buffers=1))])
+@pytest.mark.parametrize("N,cfg", [(1024, None), (520, m.Config(kernel=2, n_tile=512, acc_buffers=1))])
 def test_plan_stacks_short_blocks(dev, bR, pattern, param, N, cfg):
     """16- and 32-row blocks whose block rows share their columns (band,
     block-diagonal) run stacked as 64-row blocks: the same product as the
@@ -329,10 +329,11 @@ def test_plan_stacks_short_blocks(dev, bR, pattern, param, N, cfg):
     plan.close()
 
 
-@pytest.mark.parametrize("M,pattern,density", [(4096, m.PATTERN_RANDOM, 0.05),        # columns rarely shared
-                                               (4096 + 16, m.PATTERN_BAND, 0.2)])     # M not a multiple of 64
-def test_plan_does_not_stack(dev, M, pattern, density):
-    K, N = 4096, 256
+@pytest.mark.parametrize("M,pattern,density,N", [(4096, m.PATTERN_RANDOM, 0.05, 1024),     # columns rarely shared
+                                                 (4096 + 16, m.PATTERN_BAND, 0.2, 1024),  # M not a multiple of 64
+                                                 (4096, m.PATTERN_BAND, 0.2, 512)])       # N too small to pay
+def test_plan_does_not_stack(dev, M, pattern, density, N):
+    K = 4096
     rp, ci, vals, A = _int_bcsr(M, K, 16, pattern, density, 8, 13, dev)
     B = torch.from_numpy(np.random.default_rng(14).integers(-2, 3, (K, N)).astype(np.float32)).to(dev).half()
     plan = m.BcsrPlan(A, N)
@@ -346,7 +347,7 @@ def test_plan_stacked_bf16_in_cuda_graph(dev):
     """A stacked run is two launches (the copy into 64-row blocks, then the
     pipeline); captured in a graph and replayed it matches the eager product."""
     M = K = 8192
-    N = 512
+    N = 1024
     rp, ci, vals, A = _int_bcsr(M, K, 16, m.PATTERN_BAND, 0.2, 8, 15, dev, m.DType.BF16)
     B = torch.from_numpy(np.random.default_rng(16).integers(-2, 3, (K, N)).astype(np.float32)).to(dev).bfloat16()
     plan = m.BcsrPlan(A, N)
