@@ -391,12 +391,46 @@ def run_ours(args, world, rank, local):
         return tuner.config_name(c)
 
     stream = torch.cuda.current_stream()
+    graph_note = {"ok": True, "why": ""}
+
+    def capture(probs, cfg, steps):
+        """`steps` launches captured in one CUDA graph, or None if capture fails.
+        Replaying it issues the launches with no host work between them, so a
+        loop of launches a few microseconds long is not bound by the Python
+        call that issues each one."""
+        if not graph_note["ok"]:
+            return None
+        try:
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                for i in range(3):   # warm-up on a side stream, as capture wants
+                    launch(probs[i % len(probs)], cfg, stream=side)
+            torch.cuda.current_stream().wait_stream(side)
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="relaxed"):
+                cs = torch.cuda.current_stream()
+                for i in range(steps):
+                    launch(probs[i % len(probs)], cfg, stream=cs)
+            g.replay()   # first replay uploads the graph
+            torch.cuda.synchronize()
+            return g
+        except Exception as e:   # time eager launches from here on
+            graph_note.update(ok=False, why=str(e).splitlines()[0][:200])
+            sys.stderr.write("graph capture failed (%s); timing eager launches\n" % graph_note["why"])
+            torch.cuda.synchronize()
+            return None
 
     def time_loop(probs, cfg, steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g = capture(probs, cfg, steps)
         e0.record(stream)
-        for i in range(steps):
-            launch(probs[i % len(probs)], cfg)
+        if g is not None:
+            g.replay()
+        else:
+            for i in range(steps):
+                launch(probs[i % len(probs)], cfg)
         e1.record(stream)
         e1.synchronize()
         return e0.elapsed_time(e1) / steps
@@ -480,13 +514,15 @@ def run_ours(args, world, rank, local):
         cfg = results[tuned]["cands"][prev["config"]["kernel_config"]]
         probs = prepared[tuned]
 
-    # warm-up, then exactly K timed steps on the tuned configuration
+    # warm-up, then exactly K timed steps on the tuned configuration: the K
+    # launches are captured in one CUDA graph beforehand and replayed once
     t_warm = time.time()
     w = 0
     while w < args.warmup or time.time() - t_warm < 1.0:
         launch(probs[w % len(probs)], cfg)
         w += 1
     torch.cuda.synchronize()
+    timed_graph = capture(probs, cfg, args.steps)
     barrier(world)
     torch.cuda.synchronize()
     sampler.mark("timed_start")
@@ -495,8 +531,11 @@ def run_ours(args, world, rank, local):
     # (ncu --nvtx --nvtx-include "bench_timed/")
     torch.cuda.nvtx.range_push("bench_timed")
     g0.record(stream)
-    for i in range(args.steps):
-        launch(probs[i % len(probs)], cfg)
+    if timed_graph is not None:
+        timed_graph.replay()
+    else:
+        for i in range(args.steps):
+            launch(probs[i % len(probs)], cfg)
     g1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
@@ -616,6 +655,9 @@ def run_ours(args, world, rank, local):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
                        "nnzb": nnzb,
+                       "timed_loop": ("the K launches captured in one CUDA graph before the timed region and "
+                                      "replayed once (the candidates' loops likewise)") if graph_note["ok"]
+                       else "eager launches (graph capture failed: %s)" % graph_note["why"],
                        "inputs_ready": ("plan runs with SPMM_RUN_INPUTS_READY: no kernel in the timed loop writes "
                                         "A or B, so a launch copies and multiplies its first items while the "
                                         "previous step finishes, and waits for it before claiming queued work "
