@@ -65,6 +65,17 @@ long long spmm_host_dense_to_csr(const void* A_half, int rows, int cols, int* hd
 spmm_status spmm_bcsr_plan_items(const int* row_ptr, int MB, int ntiles, long long slots, int* n_items,
                                  int* n_groups, int* items, int* pair, int* parts);
 
+/* The structure a per-matrix plan stacks 16- or 32-row blocks into (no GPU):
+ * each group of `rows_per_stack` block rows becomes one row whose columns are
+ * the sorted union of the group's block columns; s_map holds, per stacked
+ * block and member row, the source block index or -1 (the block is zeros
+ * there). s_row_ptr: MB / rows_per_stack + 1 entries; s_col_idx:
+ * *stacked_blocks; s_map: *stacked_blocks * rows_per_stack. Pass NULL arrays
+ * to get *stacked_blocks first. SPMM_ERR_INVALID_ARG when a block row repeats
+ * a column. */
+spmm_status spmm_bcsr_stack_structure(const int* row_ptr, const int* col_idx, int MB, int rows_per_stack,
+                                      long long* stacked_blocks, int* s_row_ptr, int* s_col_idx, int* s_map);
+
 /* Matrix Market files (.mtx): what the reference's generator writes through
  * scipy's mmwrite (matrix_generator.py:100-108). Coordinate (real, integer or
  * pattern; general, symmetric or skew-symmetric) and array (real, general)

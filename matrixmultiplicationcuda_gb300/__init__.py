@@ -51,6 +51,7 @@ from .host import (  # noqa: F401
     generate_matrix,
     gen_structure,
     plan_items,
+    stack_structure,
     gen_values,
     gen_dense,
     host_dense_to_bcsr,

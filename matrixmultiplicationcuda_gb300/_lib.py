@@ -135,6 +135,7 @@ _SIGS = {
     "spmm_structure_features_host": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp]),
     "spmm_generate_matrix": (c_int, [c_int, c_int, c_double, c_char_p, c_int, c_uint, c_vp]),
     "spmm_gen_structure": (c_ll, [c_int, c_int, c_int, c_int, c_double, c_double, c_ull, c_vp, c_vp]),
+    "spmm_bcsr_stack_structure": (c_int, [c_vp, c_vp, c_int, c_int, ctypes.POINTER(c_ll), c_vp, c_vp, c_vp]),
     "spmm_bcsr_plan_items": (c_int, [c_vp, c_int, c_int, c_ll, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_vp,
                                      c_vp, c_vp]),
     "spmm_gen_values": (None, [c_ll, c_int, c_int, c_int, c_ull, c_vp]),

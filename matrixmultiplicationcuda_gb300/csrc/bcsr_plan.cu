@@ -389,3 +389,21 @@ extern "C" spmm_status spmm_bcsr_plan_items(const int* row_ptr, int MB, int ntil
     for (size_t g = 0; g < group_parts.size(); ++g) parts[g] = group_parts[g];
   return SPMM_OK;
 }
+
+extern "C" spmm_status spmm_bcsr_stack_structure(const int* row_ptr, const int* col_idx, int MB, int rows_per_stack,
+                                                 long long* stacked_blocks, int* s_row_ptr, int* s_col_idx,
+                                                 int* s_map) {
+  if (!row_ptr || MB < 0 || rows_per_stack < 1 || MB % rows_per_stack || !stacked_blocks)
+    return fail(SPMM_ERR_INVALID_ARG, "bad stacking arguments");
+  for (int r = 0; r < MB; ++r)
+    if (row_ptr[r + 1] < row_ptr[r]) return fail(SPMM_ERR_INVALID_ARG, "row_ptr must not decrease");
+  if (row_ptr[MB] > 0 && !col_idx) return fail(SPMM_ERR_INVALID_ARG, "null col_idx");
+  std::vector<int> srp, sci, smap;
+  if (!build_stack(row_ptr, col_idx, MB, rows_per_stack, &srp, &sci, &smap))
+    return fail(SPMM_ERR_INVALID_ARG, "a block row repeats a column");
+  *stacked_blocks = (long long)sci.size();
+  if (s_row_ptr) std::copy(srp.begin(), srp.end(), s_row_ptr);
+  if (s_col_idx) std::copy(sci.begin(), sci.end(), s_col_idx);
+  if (s_map) std::copy(smap.begin(), smap.end(), s_map);
+  return SPMM_OK;
+}

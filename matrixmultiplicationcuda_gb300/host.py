@@ -51,6 +51,26 @@ def plan_items(row_ptr, ntiles, slots):
     return items[:n.value], pair[:n.value], parts[:g.value]
 
 
+def stack_structure(row_ptr, col_idx, rows_per_stack):
+    """The stacked structure a plan builds for 16- or 32-row blocks
+    (spmm_bcsr_stack_structure): (row_ptr, col_idx, map [blocks, rows_per_stack]
+    of source block indices or -1)."""
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    ci = np.ascontiguousarray(col_idx, np.int32)
+    if ci.size == 0:
+        ci = np.zeros(1, np.int32)
+    MB = len(rp) - 1
+    n = ctypes.c_longlong()
+    check(lib().spmm_bcsr_stack_structure(_vp(rp), _vp(ci), MB, int(rows_per_stack), ctypes.byref(n), None, None,
+                                          None))
+    srp = np.empty(MB // rows_per_stack + 1, np.int32)
+    sci = np.empty(max(n.value, 1), np.int32)
+    smap = np.empty(max(n.value, 1) * rows_per_stack, np.int32)
+    check(lib().spmm_bcsr_stack_structure(_vp(rp), _vp(ci), MB, int(rows_per_stack), ctypes.byref(n), _vp(srp),
+                                          _vp(sci), _vp(smap)))
+    return srp, sci[:n.value], smap[:n.value * rows_per_stack].reshape(-1, rows_per_stack)
+
+
 def gen_values(nnzb, bR, bC=16, dist=DIST_UNIFORM, seed=2):
     out = np.empty(nnzb * bR * bC, np.float32)
     lib().spmm_gen_values(nnzb, bR, bC, dist, seed, _vp(out))

@@ -110,3 +110,60 @@ def test_plan_items_rejects():
     assert e.value.status == m.Status.INVALID_ARG
     with pytest.raises(m.SpmmError):
         m.plan_items(np.array([0, 5], np.int32), 0, 304)
+
+
+def restated_stack(rp, ci, st):
+    """Stacking in plain Python: per group of `st` block rows, the sorted union
+    of their columns, and per union column the member rows' block indices."""
+    srp, sci, smap = [0], [], []
+    for g in range((len(rp) - 1) // st):
+        cols = {}
+        for t in range(st):
+            r = g * st + t
+            for b in range(rp[r], rp[r + 1]):
+                cols.setdefault(int(ci[b]), [-1] * st)[t] = b
+        for c in sorted(cols):
+            sci.append(c)
+            smap.append(cols[c])
+        srp.append(len(sci))
+    return np.array(srp, np.int32), np.array(sci, np.int32), np.array(smap, np.int32).reshape(-1, st)
+
+
+STACK_CASES = [
+    ("band 16", 4096, 16, m.PATTERN_BAND, 0.2, 8),
+    ("band 32", 4096, 32, m.PATTERN_BAND, 0.2, 8),
+    ("blockdiag 16", 4096, 16, m.PATTERN_BLOCKDIAG, 0.2, 256),
+    ("random 16", 4096, 16, m.PATTERN_RANDOM, 0.05, 0),
+    ("log-normal 32", 4096, 32, m.PATTERN_LOGNORMAL, 0.05, 1.5),
+]
+
+
+@pytest.mark.parametrize("name,M,bR,pattern,density,param", STACK_CASES, ids=[c[0] for c in STACK_CASES])
+def test_stack_structure(name, M, bR, pattern, density, param):
+    rp, ci = m.gen_structure(M, M, bR, pattern, density, param, seed=21)
+    st = 64 // bR
+    srp, sci, smap = m.stack_structure(rp, ci, st)
+    rrp, rci, rmap = restated_stack(rp, ci, st)
+    assert np.array_equal(srp, rrp) and np.array_equal(sci, rci) and np.array_equal(smap, rmap)
+    # every block lands once, in its member row's slot of its own column
+    seen = np.zeros(len(ci), np.int64)
+    for g in range(len(srp) - 1):
+        cols = sci[srp[g]:srp[g + 1]]
+        assert np.all(np.diff(cols) > 0)
+        for j in range(srp[g], srp[g + 1]):
+            for t, b in enumerate(smap[j]):
+                if b >= 0:
+                    seen[b] += 1
+                    assert rp[g * st + t] <= b < rp[g * st + t + 1] and ci[b] == sci[j]
+    assert np.all(seen == 1)
+    if pattern in (m.PATTERN_BAND, m.PATTERN_BLOCKDIAG):
+        assert len(sci) * 100 <= len(ci) * 60      # the plan would stack these
+    if pattern == m.PATTERN_RANDOM:
+        assert len(sci) * 100 > len(ci) * 60       # and not this one
+
+
+def test_stack_structure_rejects():
+    with pytest.raises(m.SpmmError):
+        m.stack_structure(np.array([0, 2, 2, 2, 2], np.int32), np.array([3, 3], np.int32), 4)   # repeated column
+    with pytest.raises(m.SpmmError):
+        m.stack_structure(np.array([0, 1, 2, 3], np.int32), np.array([0, 1, 2], np.int32), 2)   # 3 rows, stacks of 2
