@@ -49,6 +49,14 @@ SEED = 20240
 WORKLOAD = ("A 16384x16384, 64x16 blocks, random 2% block density, values N(0,1)*10^U[-3,3] "
             "per block; B 16384x512 N(0,1); C fp32")
 METRIC = "BCSR SpMM TFLOP/s (nonzero-block FLOPs), tuned mixed precision vs plain FP16"
+# Problem copies used round-robin by the GPU arms: 6 x 60.8 MB = 365 MB, over
+# 2.5x the 129 MB L2, so no step reads another step's inputs from L2.
+COPIES = 6
+DATA = "synthetic (seeded generators)"
+# The workload, the same in both arms (how each arm runs it is in its own keys).
+CONFIG = {"workload": WORKLOAD,
+          "l2": "GPU steps rotate over %d problem copies (365 MB, > 2.5x L2); the CPU arm's sample "
+                "is its own" % COPIES}
 # Documented normwise error bars vs FP64 (tests/test_gpu_precision.py).
 ERROR_BAR = {"f16": 2e-3, "bf16": 1e-2, "f16_split": 2e-6, "e4m3": 8e-2}
 TARGET_ERR = 1e-2
@@ -193,10 +201,9 @@ def barrier(world):
         dist.barrier()
 
 
-def cpu_sample_rows(rp, ci, vals_f32, B_half_bits, rows, row0):
+def cpu_sample_rows(rp, ci, vals_f32, rows, row0):
     """Dense fp16 rows [row0, row0+rows) of A (what the reference host multiply reads)."""
-    K16 = K
-    A = np.zeros((rows, K16), np.float16)
+    A = np.zeros((rows, K), np.float16)
     br0, br1 = row0 // BR, (row0 + rows + BR - 1) // BR
     blocks = vals_f32.reshape(-1, BR, 16)
     for br in range(br0, br1):
@@ -219,7 +226,7 @@ def useful_flops_rows(rp, row0, rows):
 def cpu_reference_rate(rp, ci, vals, Bbits, rows, threads, min_seconds=0.0, row0=0):
     """TFLOP/s (nonzero-block) of the restated reference host multiply on `rows` rows."""
     from oracle import oracle
-    A = cpu_sample_rows(rp, ci, vals, Bbits, rows, row0)
+    A = cpu_sample_rows(rp, ci, vals, rows, row0)
     done, t = 0.0, 0.0
     while True:
         t0 = time.perf_counter()
@@ -231,49 +238,68 @@ def cpu_reference_rate(rp, ci, vals, Bbits, rows, threads, min_seconds=0.0, row0
     return done / t / 1e12, t
 
 
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 # ------------------------------------------------------------------------------------
 def run_reference(args, world, rank):
+    """The reference's host multiply (cpu_matmul_ref, nvbench_main.cu:78-91, in the
+    oracle's restatement) on every host thread, over a bounded sample of output
+    rows per step. Its inputs come from the oracle's restatement of the synthetic
+    generators (bit-identical to the library's, pinned by the CPU tests), so this
+    arm loads nothing of the library."""
     if rank != 0:
         return
-    import matrixmultiplicationcuda_gb300 as m
-    rp, ci = make_structure()
+    from oracle import oracle
+    rp, ci = oracle.gen_structure(M, K, BR, oracle.PATTERN_RANDOM, DENSITY, 0, seed=SEED)
     nnzb = len(ci)
-    vals = m.gen_values(nnzb, BR, 16, m.DIST_SCALED_NORMAL, seed=SEED + 1).astype(np.float16).astype(np.float32)
-    B = m.gen_dense(K, N, m.DIST_NORMAL, seed=SEED + 2).astype(np.float16)
-    threads = os.cpu_count() or 1
-    rows = 64 * threads          # bounded sample per step, ~1 s on 16 cores
+    vals = oracle.gen_values(nnzb, BR, 16, oracle.DIST_SCALED_NORMAL, seed=SEED + 1)
+    vals = vals.astype(np.float16).astype(np.float32)
+    B = oracle.gen_dense(K, N, oracle.DIST_NORMAL, seed=SEED + 2).astype(np.float16)
+    threads = host_threads()
+    rows = 64 * threads          # bounded sample per step: about 0.4 s on 16 Arm cores
     for i in range(args.warmup):
-        cpu_reference_rate(rp, ci, vals, B.view(np.uint16), min(rows, 256), threads, row0=(i * 977) % (M - rows))
+        r0 = (i * 977) % (M - rows)
+        r0 -= r0 % BR
+        cpu_reference_rate(rp, ci, vals, B.view(np.uint16), min(rows, 256), threads, row0=r0)
     t_total, f_total = 0.0, 0.0
     for i in range(args.steps):
         r0 = (i * 1931) % (M - rows)
         r0 -= r0 % BR
-        A = cpu_sample_rows(rp, ci, vals, B.view(np.uint16), rows, r0)
-        from oracle import oracle
+        A = cpu_sample_rows(rp, ci, vals, rows, r0)
         t0 = time.perf_counter()
         oracle.cpu_matmul_ref(A.view(np.uint16), B.view(np.uint16), threads=threads)
         t_total += time.perf_counter() - t0
         f_total += useful_flops_rows(rp, r0, rows)
     value = f_total / t_total / 1e12
-    wmma = reference_wmma_gpu(rp, ci, vals, B)
+    wmma = None if args.no_wmma else reference_wmma_gpu(rp, ci, vals, B)
+    sample = ("%d of %d output rows per step (rows [r0, r0 + %d), r0 moving over the matrix), the "
+              "reference host multiply (dense i-k-j over all K, fp32, zeros multiplied too) split by rows "
+              "over %d threads; the rate counts the sample's nonzero-block FLOPs" % (rows, M, rows, threads))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "sample": "%d output rows per step" % rows},
+            "data": DATA, "config": dict(CONFIG),
+            "us_per_output_row": 1e6 * t_total / (args.steps * rows),
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-                             "sample": "%d of %d output rows per step, reference host multiply "
-                                       "(dense i-k-j, fp32) split by rows over %d threads" % (rows, M, threads)},
+                             "sample": sample},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0,
             "reference_wmma_gpu": wmma}
     print(json.dumps(line))
 
 
 def reference_wmma_gpu(rp, ci, vals, B, reps=20):
-    """The reference's own WMMA kernel for 64x16 blocks (sparseMatrixMulTensor64x16,
-    src/cuda_kernels.cu:618-695, built unmodified for sm_103a), launched with the
-    reference harness's grid on the same workload, timed with CUDA events on a
-    cold L2. None when no GPU or no reference build is present."""
+    """Context beside the CPU rate: the reference's own WMMA kernel for 64x16 blocks
+    (sparseMatrixMulTensor64x16, src/cuda_kernels.cu:618-695, built unmodified for
+    sm_103a), launched with the reference harness's grid on the same product: timed
+    alone after an L2 flush (the reference harness's cold timing) and back to back
+    over six rotating copies (the timing of the library's own step). None when no
+    GPU or no reference build is present."""
     try:
         import torch
         from oracle import oracle
@@ -283,48 +309,51 @@ def reference_wmma_gpu(rp, ci, vals, B, reps=20):
         return None
     dev = torch.device("cuda", 0)
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
-    d = [t(rp), t(ci), t(vals.astype(np.float16)), t(B)]
-    C = torch.empty((M, N), dtype=torch.float32, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     st = torch.cuda.current_stream().cuda_stream
-    launch = lambda: oracle.ref_wmma_launch("sparseMatrixMulTensor64x16", d[0].data_ptr(), d[1].data_ptr(),
-                                            d[2].data_ptr(), d[3].data_ptr(), C.data_ptr(), M, N, st)
-    for _ in range(3):
-        launch()
-    ts = []
-    for k in range(reps):
-        flush.fill_(k & 0xff)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        launch()
-        e1.record()
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1) * 1e3)
-    us = float(np.mean(ts))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def cold(launch):
+        for _ in range(3):
+            launch(0)
+        ts = []
+        for k in range(reps):
+            flush.fill_(k & 0xff)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            launch(0)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e3)
+        return float(np.mean(ts))
+
+    copies = [[t(rp), t(ci), t(vals.astype(np.float16)), t(B), torch.empty((M, N), dtype=torch.float32, device=dev)]
+              for _ in range(COPIES)]
+    launch = lambda i: oracle.ref_wmma_launch("sparseMatrixMulTensor64x16", *[x.data_ptr() for x in copies[i % COPIES]],
+                                              M, N, st)
+    us = cold(launch)
+    for i in range(COPIES):
+        launch(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    loops = 60
+    e0.record()
+    for i in range(loops):
+        launch(i)
+    e1.record()
+    torch.cuda.synchronize()
+    us_b2b = e0.elapsed_time(e1) * 1e3 / loops
     flops = 2.0 * len(ci) * BR * 16 * N
     out = {"kernel": "sparseMatrixMulTensor64x16", "us": us, "tflops": flops / (us * 1e-6) / 1e12,
+           "back_to_back_us": us_b2b, "back_to_back_tflops": flops / (us_b2b * 1e-6) / 1e12,
            "grid": "(N/32, M/64) warps of 32 threads, as the reference harness launches it"}
-    # the 1024^2 16x16 case through the reference's own generator and BCSR build
-    import matrixmultiplicationcuda_gb300 as m
-    A1 = m.generate_matrix(1024, 1024, 0.9, "blockrandom", 16, 123).astype(np.float16)
-    B1 = m.generate_matrix(1024, 1024, 0.0, "random", 16, 456).astype(np.float16)
-    hdr, idx, data = m.host_dense_to_bcsr(A1.view(np.uint16), 16, 16)
-    d1 = [t(hdr), t(idx), t(data.view(np.float16)), t(B1)]
-    C1 = torch.empty((1024, 1024), dtype=torch.float32, device=dev)
-    launch1 = lambda: oracle.ref_wmma_launch("sparseMatrixMulTensor", d1[0].data_ptr(), d1[1].data_ptr(),
-                                             d1[2].data_ptr(), d1[3].data_ptr(), C1.data_ptr(), 1024, 1024, st)
-    for _ in range(3):
-        launch1()
-    ts = []
-    for k in range(reps):
-        flush.fill_(k & 0xff)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        launch1()
-        e1.record()
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1) * 1e3)
-    us1 = float(np.mean(ts))
+    del copies
+    # the 1024^2 16x16 case through the reference generator and BCSR build (restated)
+    A1 = oracle.generate_matrix(1024, 1024, 0.9, "blockrandom", 16, 123)
+    B1 = oracle.f32_to_f16(oracle.generate_matrix(1024, 1024, 0.0, "random", 16, 456))
+    hdr, idx, data = oracle.bcsr(oracle.f32_to_f16(A1), 16, 16)
+    d1 = [t(hdr), t(idx), t(data), t(B1), torch.empty((1024, 1024), dtype=torch.float32, device=dev)]
+    launch1 = lambda i: oracle.ref_wmma_launch("sparseMatrixMulTensor", *[x.data_ptr() for x in d1], 1024, 1024, st)
+    us1 = cold(launch1)
     f1 = 2.0 * len(idx) * 16 * 16 * 1024
     return {"A16384_64x16_N512": out,
             "A1024_16x16_N1024": {"kernel": "sparseMatrixMulTensor", "us": us1, "tflops": f1 / (us1 * 1e-6) / 1e12,
@@ -350,7 +379,8 @@ def run_ours(args, world, rank, local):
     # device copies of the problem (six, round-robin) per precision
     l2 = torch.cuda.get_device_properties(dev).L2_cache_size
     per_copy = algorithmic_bytes(nnzb, cols_touched, "f16")
-    copies = max(2, math.ceil(2.5 * l2 / per_copy))
+    copies = COPIES
+    assert copies * per_copy > 2.5 * l2, "problem copies no longer exceed 2.5x L2"
     rp_d = torch.from_numpy(rp).to(dev)
     ci_d = torch.from_numpy(ci).to(dev)
     v32 = torch.from_numpy(vals).to(dev)
@@ -511,7 +541,7 @@ def run_ours(args, world, rank, local):
         # among this run's candidates): a profiler's timings must not change the pick
         prev = json.loads(open(args.pick_from).read().strip().splitlines()[-1])
         tuned = prev["dtype"]
-        cfg = results[tuned]["cands"][prev["config"]["kernel_config"]]
+        cfg = results[tuned]["cands"][prev["run"]["kernel_config"]]
         probs = prepared[tuned]
 
     # warm-up, then exactly K timed steps on the tuned configuration: the K
@@ -614,7 +644,7 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         vh = vals.astype(np.float16).astype(np.float32)
         Bh = Bf.astype(np.float16).view(np.uint16)
-        rate, secs = cpu_reference_rate(rp, ci, vh, Bh, 192, 1, min_seconds=10.0)
+        rate, secs = cpu_reference_rate(rp, ci, vh, Bh, 192, 1, min_seconds=10.0, row0=4096)
         cpu = {"value": rate, "unit": "TFLOP/s", "cores": 1, "kind": "port",
                "sample": "192 of %d output rows, reference host multiply (dense i-k-j, fp32, "
                          "one thread), repeated for %.1f s" % (M, secs)}
@@ -646,22 +676,23 @@ def run_ours(args, world, rank, local):
         line = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": tuned, "data": "synthetic (seeded generators)",
-            "config": {"workload": WORKLOAD, "precision": tuned,
-                       "kernel_config": cfg_name(cfg),
-                       "picked_by": ("the learned cost model's pick, or the fastest per-matrix plan over the "
-                                     "tuner's tcgen05 configurations when that is faster") if not args.pick_from
-                       else "pinned to the line in %s" % os.path.basename(args.pick_from),
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "%d rotating problem copies (%.0f MB > 2.5x L2)" % (copies, copies * per_copy / 1e6),
-                       "nnzb": nnzb,
-                       "timed_loop": ("the K launches captured in one CUDA graph before the timed region and "
-                                      "replayed once (the candidates' loops likewise)") if graph_note["ok"]
-                       else "eager launches (graph capture failed: %s)" % graph_note["why"],
-                       "inputs_ready": ("plan runs with SPMM_RUN_INPUTS_READY: no kernel in the timed loop writes "
-                                        "A or B, so a launch copies and multiplies its first items while the "
-                                        "previous step finishes, and waits for it before claiming queued work "
-                                        "or writing C") if isinstance(cfg, m.BcsrPlan) else None},
+            "vs_baseline": None, "dtype": tuned, "data": DATA, "config": dict(CONFIG),
+            "us_per_output_row": 1e3 * ms_step / M,
+            "run": {"precision": tuned,
+                    "kernel_config": cfg_name(cfg),
+                    "picked_by": ("the learned cost model's pick, or the fastest per-matrix plan over the "
+                                  "tuner's tcgen05 configurations when that is faster") if not args.pick_from
+                    else "pinned to the line in %s" % os.path.basename(args.pick_from),
+                    "parallelism": "replicas" if world > 1 else "single GPU",
+                    "copies_mb": copies * per_copy / 1e6,
+                    "nnzb": nnzb,
+                    "timed_loop": ("the K launches captured in one CUDA graph before the timed region and "
+                                   "replayed once (the candidates' loops likewise)") if graph_note["ok"]
+                    else "eager launches (graph capture failed: %s)" % graph_note["why"],
+                    "inputs_ready": ("plan runs with SPMM_RUN_INPUTS_READY: no kernel in the timed loop writes "
+                                     "A or B, so a launch copies and multiplies its first items while the "
+                                     "previous step finishes, and waits for it before claiming queued work "
+                                     "or writing C") if isinstance(cfg, m.BcsrPlan) else None},
             "plain_fp16": {"tflops": flops / plain_ms / 1e9, "ms": plain_ms,
                            "kernel_config": "library default (no tuning)"},
             "tuned_vs_plain_fp16": plain_ms / tr["ms"],
@@ -776,10 +807,213 @@ def run_profile(args):
     print("profile: %s nnzb=%d launches=%d" % (args.profile, nnzb, args.launches))
 
 
+def run_profile_families(names, launches):
+    """One representative launch sequence per kernel family, for ncu captures
+    (python bench.py --profile-family NAME[,NAME...] --launches L).
+
+    Families (seeded synthetic inputs; a few hundred MB on the device at most):
+      tc        k_bcsr_tc: A 16384^2, 64x16 blocks, random 2 %, N 512, fp16, a
+                512-column tile with one accumulator, static item stride
+      plan_c3   k_bcsr_tc on a per-matrix plan: the same product in bf16 with the
+                default tcgen05 configuration (256-column tile, five-group ring,
+                two accumulators), items heaviest first from the plan's queue
+      plan_c3_512  the same product in fp16 on a plan with a 512-column tile and
+                one accumulator (one item per CTA), each launch started with
+                SPMM_RUN_INPUTS_READY after the first
+      tc_split  k_bcsr_tc in split fp16 (three MMAs per block), same product
+      mma_e4m3  k_bcsr_mma: the same product in e4m3 with per-block scales
+      mma16     k_bcsr_mma: A 8192^2, 16x16 blocks, random 5 %, N 1024, fp16
+      batch     k_bcsr_tc_batch: the 64-product uneven workload, one launch
+      convert   k_dense_to_bcsr (count and fill) + k_scan_counts: dense fp16
+                8192 x 8192 (134 MB) with 16x16 blocks at 5 %
+      quantize  k_to_f16 / k_to_bf16 / k_absmax / k_to_e4m3: 64 M fp32 values
+      mlp       the cost model's forward / backward / AdamW kernels, batch 2000
+      hybrid    k_bcsr_tc with the CSR pass in its epilogue (spmm_hcsr_mm): A 4096^2
+                (10 % dense 16x16 blocks + 2 % scattered entries), threshold 0.5,
+                N 1024
+      hybrid_plan  the same product planned: CSR entries as gather blocks
+      csr       k_csr_mm on the same matrix's entries, all as CSR
+      tc64      k_bcsr_tc64 (64-row blocks, M=64 UMMAs, one CTA per SM): the tc
+                product in fp16 and in split fp16, 256-column tile
+      plan      k_bcsr_tc on a per-matrix plan: A 8192^2, 64x16 blocks, log-normal
+                rows (5 %, CV 1.5), N 512, bf16, 256-column tile (rows far above
+                the average load split into parts)
+      dense     k_dense_tc: the native dense comparator, A 8192 x 8192, B 8192 x 1024, fp16
+      gen       the GPU generators: k_gen_structure + k_gen_values for the tc
+                product's structure (A 16384^2, 64x16, 2 %), k_gen_dense for B
+                (16384 x 512), k_gen_matrix (reference blockrandom, 8192^2 fp16)
+    Each family runs `--launches` times after one warm-up, then synchronises and
+    checks the device error word.
+    """
+    only = set(names.split(","))
+    L = launches
+    import torch
+    import matrixmultiplicationcuda_gb300 as m
+    from matrixmultiplicationcuda_gb300 import costmodel
+    dev = torch.device("cuda", 0)
+
+    def c3(dtype):
+        M = K = 16384
+        N = 512
+        rp, ci = m.gen_structure(M, K, 64, m.PATTERN_RANDOM, 0.02, 0, seed=20240)
+        vals = m.gen_values(len(ci), 64, 16, m.DIST_SCALED_NORMAL, seed=20241)
+        Bf = m.gen_dense(K, N, m.DIST_NORMAL, seed=20242)
+        A = m.BCSR.from_host(M, K, 64, rp, ci, vals, dtype, device=dev)
+        Bq, Blo, Bs = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), dtype)
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        return A, Bq.view(K, N), (Blo.view(K, N) if Blo is not None else None), \
+            (float(Bs[0]) if Bs is not None else 1.0), C
+
+    def run(fn):
+        fn()
+        torch.cuda.synchronize()
+        for _ in range(L):
+            fn()
+        torch.cuda.synchronize()
+        m.device_error_check()
+
+    if "tc" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16)
+        cfg = m.Config(kernel=2, n_tile=512, acc_buffers=1)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=cfg))
+        print("tc: nnzb=%d" % A.nnzb)
+    if "tc_split" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16_SPLIT)
+        cfg = m.Config(kernel=2, n_tile=256, acc_buffers=2, stages=2)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=cfg, B_lo=Blo))
+        print("tc_split: nnzb=%d" % A.nnzb)
+    if "mma_e4m3" in only:
+        A, B, Blo, bs, C = c3(m.DType.E4M3)
+        cfg = m.Config(kernel=1, n_tile=128, stages=4)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=cfg, b_scale=bs))
+        print("mma_e4m3: nnzb=%d" % A.nnzb)
+    if "mma16" in only:
+        M = K = 8192
+        N = 1024
+        rp, ci = m.gen_structure(M, K, 16, m.PATTERN_RANDOM, 0.05, 0, seed=7)
+        vals = m.gen_values(len(ci), 16, 16, m.DIST_UNIFORM, seed=8)
+        A = m.BCSR.from_host(M, K, 16, rp, ci, vals, m.DType.F16, device=dev)
+        B = torch.from_numpy(m.gen_dense(K, N, m.DIST_UNIFORM, seed=9)).to(dev).half()
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        cfg = m.Config(kernel=1, n_tile=256, stages=4)
+        run(lambda: m.spmm(A, B, N=N, C=C, cfg=cfg))
+        print("mma16: nnzb=%d" % A.nnzb)
+    if "batch" in only:
+        probs = []
+        for sp in m.uneven_batch_specs(64, seed=2024):
+            rp, ci, vals, Bf = m.make_problem(sp)
+            A = m.BCSR.from_host(sp["M"], sp["K"], sp["bR"], rp, ci, vals, m.DType.F16, device=dev)
+            probs.append((A, torch.from_numpy(Bf).to(dev).half(),
+                          torch.empty((sp["M"], sp["N"]), dtype=torch.float32, device=dev)))
+        plan = m.BatchPlan(probs)
+        run(plan.run)
+        plan.close()
+        print("batch: %d problems" % len(probs))
+    if "convert" in only:
+        M = K = 8192
+        rp, ci = m.gen_structure(M, K, 16, m.PATTERN_RANDOM, 0.05, 0, seed=11)
+        vals = m.gen_values(len(ci), 16, 16, m.DIST_UNIFORM, seed=12)
+        dense = torch.zeros((M, K), dtype=torch.float16, device=dev)
+        blocks = torch.from_numpy(vals.reshape(-1, 16, 16)).to(dev).half()
+        rows = np.repeat(np.arange(M // 16), np.diff(rp))
+        view = dense.view(M // 16, 16, K // 16, 16).permute(0, 2, 1, 3)
+        view[torch.from_numpy(rows).to(dev), torch.from_numpy(ci.astype(np.int64)).to(dev)] = blocks
+        run(lambda: m.dense_to_bcsr(dense, 16, 16))
+        print("convert: %d x %d, nnzb=%d" % (M, K, len(ci)))
+    if "quantize" in only:
+        src = torch.randn(64 << 20, device=dev) * 10
+        for dt in (m.DType.F16, m.DType.BF16, m.DType.E4M3):
+            run(lambda: m.quantize(src, dt, block_elems=1024))
+        print("quantize: %d values" % src.numel())
+    if only & {"hybrid", "hybrid_plan", "csr"}:
+        M = K = 4096
+        N = 1024
+        blocks = m.generate_matrix(M, K, 0.9, "blockrandom", 16, seed=7)
+        scatter = m.generate_matrix(M, K, 0.98, "random", 16, seed=8)
+        A = np.where(blocks != 0, blocks, scatter).astype(np.float16).view(np.uint16)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        B = t(m.gen_dense(K, N, m.DIST_UNIFORM, seed=9)).half()
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        (bh, bi, bd), (ch, cx, cd) = m.host_dense_to_hcsr(A, 0.5)
+        Ab = m.BCSR(M, K, 16, 16, t(bh), t(bi), t(bd.view(np.float16)))
+        if "hybrid" in only:
+            run(lambda: m.hcsr_mm(Ab, t(ch), t(cx), t(cd.view(np.float16)), B, N=N, C=C))
+            print("hybrid: %d blocks, %d CSR entries" % (len(bi), len(cx)))
+        if "hybrid_plan" in only:
+            plan = m.HcsrPlan(Ab, t(ch), t(cx), t(cd.view(np.float16)))
+            run(lambda: plan.run(B, N=N, C=C))
+            print("hybrid_plan: (blocks, gather blocks) =", plan.info())
+            plan.close()
+        if "csr" in only:
+            _, (rh, rx, rd) = m.host_dense_to_hcsr(A, 1.1)
+            rh, rx, rd = t(rh), t(rx), t(rd.view(np.float16))
+            run(lambda: m.csr_mm(rh, rx, rd, K, B, N=N, C=C))
+            print("csr: %d entries" % rx.numel())
+    if "plan_c3" in only:
+        A, B, Blo, bs, C = c3(m.DType.BF16)
+        plan = m.BcsrPlan(A, 512)
+        run(lambda: plan.run(A, B, C=C))
+        print("plan_c3: nnzb=%d, (items, split rows) = %s" % (A.nnzb, plan.info()[:2]))
+        plan.close()
+    if "plan_c3_512" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16)
+        plan = m.BcsrPlan(A, 512, m.Config(kernel=2, n_tile=512, acc_buffers=1))
+        torch.cuda.synchronize()   # no kernel after this writes A or B
+        run(lambda: plan.run(A, B, C=C, inputs_ready=True))
+        print("plan_c3_512: nnzb=%d, (items, split rows) = %s" % (A.nnzb, plan.info()[:2]))
+        plan.close()
+    if "tc64" in only:
+        A, B, Blo, bs, C = c3(m.DType.F16)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256)))
+        A, B, Blo, bs, C = c3(m.DType.F16_SPLIT)
+        run(lambda: m.spmm(A, B, N=512, C=C, cfg=m.Config(kernel=3, n_tile=256), B_lo=Blo))
+        print("tc64: nnzb=%d" % A.nnzb)
+    if "plan" in only:
+        M = K = 8192
+        rp, ci = m.gen_structure(M, K, 64, m.PATTERN_LOGNORMAL, 0.05, 1.5, seed=77)
+        vals = m.gen_values(len(ci), 64, 16, m.DIST_UNIFORM, seed=1)
+        A = m.BCSR.from_host(M, K, 64, rp, ci, vals, m.DType.BF16, device=dev)
+        B = torch.from_numpy(m.gen_dense(K, 512, m.DIST_UNIFORM, seed=2)).to(dev).bfloat16()
+        C = torch.empty((M, 512), dtype=torch.float32, device=dev)
+        plan = m.BcsrPlan(A, 512, m.Config(kernel=2, n_tile=256, acc_buffers=2))
+        run(lambda: plan.run(A, B, C=C))
+        print("plan: (items, split rows) =", plan.info()[:2])
+        plan.close()
+    if "dense" in only:
+        g = torch.Generator().manual_seed(0)
+        Ad = (torch.rand((8192, 8192), generator=g) * 2 - 1).half().to(dev)
+        Bd = (torch.rand((8192, 1024), generator=g) * 2 - 1).half().to(dev)
+        Cd = torch.empty((8192, 1024), dtype=torch.float32, device=dev)
+        run(lambda: m.dense_mm(Ad, Bd, C=Cd))
+        print("dense: 8192 x 8192 x 1024")
+    if "gen" in only:
+        def gen():
+            rp, ci = m.gpu_gen_structure(16384, 16384, 64, m.PATTERN_RANDOM, 0.02, 0, seed=20240, device=dev)
+            m.gpu_gen_values(ci.numel(), 64, 16, m.DIST_SCALED_NORMAL, seed=20241, device=dev)
+            m.gpu_gen_dense(16384, 512, m.DIST_NORMAL, seed=20242, device=dev)
+            m.gpu_generate_matrix(8192, 8192, 0.9, "blockrandom", 16, seed=7, device=dev)
+        run(gen)
+        print("gen: done")
+    if "mlp" in only:
+        s = costmodel.shape()
+        rng = np.random.default_rng(0)
+        p = costmodel.init_params(s, np.zeros(s.in_, np.float32), np.ones(s.in_, np.float32))
+        net = costmodel.MLP(s, p, device=dev)
+        X = torch.from_numpy(rng.standard_normal((2000, s.in_)).astype(np.float32)).to(dev)
+        T = torch.from_numpy(rng.standard_normal((2000, s.out)).astype(np.float32)).to(dev)
+        Mk = torch.ones_like(T)
+        run(lambda: net.forward(X))
+        run(lambda: net.loss_grad(X, T, Mk))
+        print("mlp: batch 2000")
+
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile", default=None, choices=["f16", "bf16", "e4m3", "f16_split"])
     ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--profile-family", default=None,
+                    help="comma-separated kernel families to launch for a profiler (see run_profile_families)")
     ap.add_argument("--kernel", type=int, default=0)
     ap.add_argument("--n-tile", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)
@@ -793,10 +1027,13 @@ def main():
     ap.add_argument("--pick-from", default=None,
                     help="run the precision and configuration named by an earlier run's JSON line (for profiling)")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-wmma", action="store_true", help="reference arm: skip the reference WMMA kernel timing")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
-    if args.profile:
+    if args.profile_family:
+        run_profile_families(args.profile_family, args.launches)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args, world, rank)

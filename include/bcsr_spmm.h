@@ -119,14 +119,46 @@ spmm_status sparseMatrixMulTensor32x16_launch(const int* hdr, const int* idx, co
 spmm_status sparseMatrixMulTensor64x16_launch(const int* hdr, const int* idx, const void* data,
                                               const void* B, float* C, unsigned M, unsigned N,
                                               unsigned K, void* stream);
-/* Variant kernels of the reference compute the same product with other warp
- * splits; each maps onto the launcher of its block shape:
- *   _v2 (:370-417), _v3 (:423-489), _v1_improved (:495-547)          -> 16x16
- *   32x16_v2 (:1001-1050), 32x16_shared (:768-845),
- *   32x16_shared_vectorized (:853-934), 32x16_v2_shared_vectorized (:1056-1166) -> 32x16
- *   64x16_v2 (:939-996)                                               -> 64x16
- *   Adaptive / Adaptive32x16 / Adaptive64x16 (:1171-1363): colBlocksPerRow is
- *   accepted and ignored (the persistent schedule balances the columns). */
+/* The reference's variant kernels compute the same product with other warp
+ * splits or staging. Each has a launcher of its own name, with the argument
+ * list above, that runs this library's pipeline for its block shape. */
+/* sparseMatrixMulTensor_v2, src/cuda_kernels.cu:370-417 (16x16) */
+spmm_status sparseMatrixMulTensor_v2_launch(const int* hdr, const int* idx, const void* data,
+                                            const void* B, float* C, unsigned M, unsigned N,
+                                            unsigned K, void* stream);
+/* sparseMatrixMulTensor_v3, src/cuda_kernels.cu:423-489 (16x16) */
+spmm_status sparseMatrixMulTensor_v3_launch(const int* hdr, const int* idx, const void* data,
+                                            const void* B, float* C, unsigned M, unsigned N,
+                                            unsigned K, void* stream);
+/* sparseMatrixMulTensor_v1_improved, src/cuda_kernels.cu:495-547 (16x16) */
+spmm_status sparseMatrixMulTensor_v1_improved_launch(const int* hdr, const int* idx, const void* data,
+                                                     const void* B, float* C, unsigned M, unsigned N,
+                                                     unsigned K, void* stream);
+/* sparseMatrixMulTensor32x16_v2, src/cuda_kernels.cu:1001-1050 (32x16) */
+spmm_status sparseMatrixMulTensor32x16_v2_launch(const int* hdr, const int* idx, const void* data,
+                                                 const void* B, float* C, unsigned M, unsigned N,
+                                                 unsigned K, void* stream);
+/* sparseMatrixMulTensor32x16_shared, src/cuda_kernels.cu:768-845 (32x16) */
+spmm_status sparseMatrixMulTensor32x16_shared_launch(const int* hdr, const int* idx, const void* data,
+                                                     const void* B, float* C, unsigned M, unsigned N,
+                                                     unsigned K, void* stream);
+/* sparseMatrixMulTensor32x16_shared_vectorized, src/cuda_kernels.cu:853-934 (32x16) */
+spmm_status sparseMatrixMulTensor32x16_shared_vectorized_launch(const int* hdr, const int* idx,
+                                                                const void* data, const void* B, float* C,
+                                                                unsigned M, unsigned N, unsigned K,
+                                                                void* stream);
+/* sparseMatrixMulTensor32x16_v2_shared_vectorized, src/cuda_kernels.cu:1056-1166 (32x16) */
+spmm_status sparseMatrixMulTensor32x16_v2_shared_vectorized_launch(const int* hdr, const int* idx,
+                                                                   const void* data, const void* B,
+                                                                   float* C, unsigned M, unsigned N,
+                                                                   unsigned K, void* stream);
+/* sparseMatrixMulTensor64x16_v2, src/cuda_kernels.cu:939-996 (64x16) */
+spmm_status sparseMatrixMulTensor64x16_v2_launch(const int* hdr, const int* idx, const void* data,
+                                                 const void* B, float* C, unsigned M, unsigned N,
+                                                 unsigned K, void* stream);
+/* Adaptive / Adaptive32x16 / Adaptive64x16 (src/cuda_kernels.cu:1171-1363):
+ * colBlocksPerRow is accepted and ignored (the persistent schedule balances the
+ * columns). */
 spmm_status sparseMatrixMulTensorAdaptive_launch(const int* hdr, const int* idx, const void* data,
                                                  const void* B, float* C, unsigned M, unsigned N,
                                                  unsigned colBlocksPerRow, unsigned K, void* stream);
@@ -393,10 +425,14 @@ spmm_status spmm_bcsr_plan_destroy(spmm_bcsr_plan* plan);
  * the process exits), and the call allocates nothing. The caller still passes
  * A, B and C.
  *  - fp16, bf16 and split fp16 only (E4M3 runs on a path with allocated scratch).
- *  - At most 2^30 work items (block rows x 128-column tiles): the queue
- *    counters are 32-bit. Larger problems return SPMM_ERR_SCRATCH_TOO_SMALL.
+ *  - Fewer than 2^30 work items (block rows x column tiles of the tile that
+ *    runs x split-K slices): the queue counters are 32-bit. Larger problems
+ *    return SPMM_ERR_SCRATCH_TOO_SMALL.
+ *  - K == 0 zeroes the C window (cudaMemset2DAsync, which allocates nothing).
  *  - The first call on each device looks up the array's device address
- *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *    (cudaGetSymbolAddress) and keeps it for the life of the process; make that
+ *    first call before any stream capture, and do not use this variant on a
+ *    device after cudaDeviceReset (the array may move).
  *  - Every call shares the array (one copy per device) and clears it on its
  *    stream first; calls whose launches overlap on the same GPU (for example on
  *    two streams) race on it, so serialise them.

@@ -99,6 +99,16 @@ _SIGS = {
     "sparseMatrixMulTensor_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor32x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor64x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor_v2_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor_v3_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor_v1_improved_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor32x16_v2_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor32x16_shared_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor32x16_shared_vectorized_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint,
+                                                                    c_uint, c_vp]),
+    "sparseMatrixMulTensor32x16_v2_shared_vectorized_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint,
+                                                                       c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor64x16_v2_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensorAdaptive_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensorAdaptive32x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensorAdaptive64x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_uint, c_vp]),

@@ -33,6 +33,8 @@ spmm_status fail(spmm_status st, const std::string& msg) {
 
 spmm_status host_fail(spmm_status st, const std::string& msg) { return fail(st, msg); }
 
+void clear_error() { g_last_error.clear(); }
+
 spmm_status cuda_fail(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
   return SPMM_ERR_CUDA;
@@ -414,6 +416,23 @@ spmm_status sparseMatrixMulTensor64x16_launch(const int* hdr, const int* idx, co
                                               unsigned K, void* stream) {
   return ref_launch(64, hdr, idx, data, B, C, M, N, K, stream);
 }
+// The reference's variant kernels (src/cuda_kernels.cuh:47-99) compute the
+// same product as the kernel of their block shape with another warp split or
+// staging; each name launches this library's pipeline for that block shape.
+#define SPMM_VARIANT_LAUNCHER(NAME, BR)                                                                   \
+  spmm_status NAME(const int* hdr, const int* idx, const void* data, const void* B, float* C, unsigned M, \
+                   unsigned N, unsigned K, void* stream) {                                                \
+    return ref_launch(BR, hdr, idx, data, B, C, M, N, K, stream);                                         \
+  }
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor_v2_launch, 16)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor_v3_launch, 16)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor_v1_improved_launch, 16)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_v2_launch, 32)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_shared_launch, 32)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_shared_vectorized_launch, 32)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_v2_shared_vectorized_launch, 32)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor64x16_v2_launch, 64)
+#undef SPMM_VARIANT_LAUNCHER
 spmm_status sparseMatrixMulTensorAdaptive_launch(const int* hdr, const int* idx, const void* data,
                                                  const void* B, float* C, unsigned M, unsigned N,
                                                  unsigned colBlocksPerRow, unsigned K,

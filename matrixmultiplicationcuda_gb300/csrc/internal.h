@@ -11,6 +11,7 @@ namespace spmm {
 // Thread-local last-error text; returns the status for chaining.
 spmm_status fail(spmm_status st, const std::string& msg);
 spmm_status cuda_fail(cudaError_t e, const char* what);
+void clear_error();                              // empties the calling thread's last-error text
 #define SPMM_CUDA_TRY(expr)                                   \
   do {                                                        \
     cudaError_t _e = (expr);                                  \

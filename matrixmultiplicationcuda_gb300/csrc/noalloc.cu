@@ -12,7 +12,9 @@
 // every GPU that loads the library holds it until the process exits. Host code
 // cannot use its name as a device address: the address comes from
 // cudaGetSymbolAddress, once per device, with that device current, on the
-// first call made on that device.
+// first call made on that device, and is kept for the rest of the process. A
+// cudaDeviceReset unloads the module, and the array may come back at another
+// address: do not use this variant on a device after resetting it.
 #include <cstring>
 #include <mutex>
 #include "internal.h"
@@ -55,6 +57,7 @@ extern "C" {
 
 spmm_status spmm_bcsr_mm_noalloc(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N, float* C,
                                  int ldc, const spmm_config* cfg, void* stream) {
+  clear_error();
   if (!A || !B) return fail(SPMM_ERR_INVALID_ARG, "null descriptor");
   if (A->M < 0 || A->K < 0 || N < 0) return fail(SPMM_ERR_INVALID_ARG, "negative size");
   if (A->bC != 16) return fail(SPMM_ERR_UNSUPPORTED, "block width must be 16");
@@ -65,7 +68,6 @@ spmm_status spmm_bcsr_mm_noalloc(const spmm_bcsr_desc* A, const spmm_dense_desc*
   if (A->dtype != SPMM_F16 && A->dtype != SPMM_BF16 && A->dtype != SPMM_F16_SPLIT)
     return fail(SPMM_ERR_UNSUPPORTED, "the allocation-free variant runs fp16, bf16 and split fp16");
   if (A->M == 0 || N == 0) return SPMM_OK;
-  if (A->K == 0) return fail(SPMM_ERR_UNSUPPORTED, "K == 0 is not handled by the allocation-free variant");
   if (!A->row_ptr || !C || !B->data) return fail(SPMM_ERR_INVALID_ARG, "null pointer");
   const bool split = A->dtype == SPMM_F16_SPLIT;
   if (split && (!A->vals_lo || !B->data_lo))
@@ -76,19 +78,34 @@ spmm_status spmm_bcsr_mm_noalloc(const spmm_bcsr_desc* A, const spmm_dense_desc*
   auto al = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
   if (!al(A->vals) || !al(B->data) || !al(C) || (split && (!al(A->vals_lo) || !al(B->data_lo))))
     return fail(SPMM_ERR_MISALIGNED, "A values, B and C must be 16-byte aligned");
-  // The queue counters are 32-bit and overshoot the item count by up to the
-  // grid size: a launch may hold at most 2^30 items (block rows x column tiles
-  // of at least 128 columns).
-  const long long items = (long long)(A->M / A->bR) * ((N + 127) / 128);
-  if (items > (1ll << 30))
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (A->K == 0) {
+    // no block columns: C = 0 over the window (a memset allocates nothing)
+    SPMM_CUDA_TRY(cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, A->M, s));
+    return SPMM_OK;
+  }
+  spmm_config run_cfg;
+  std::memset(&run_cfg, 0, sizeof(run_cfg));
+  if (cfg) run_cfg = *cfg;
+  run_cfg.kernel = 2;
+  run_cfg.schedule = 1;
+  // The work items the launch will hold: block rows x column tiles of the
+  // tile that runs x split-K slices. The queue counters are 32-bit and
+  // overshoot the item count by up to the grid size, so a launch may hold
+  // fewer than 2^30 items (the pipeline's own limit).
+  int nt = 0, per_sm = 0;
+  if (!tc_geometry(A->bR, A->dtype, N, run_cfg, &nt, &per_sm))
+    return fail(SPMM_ERR_UNSUPPORTED, "no tcgen05 kernel for this block height, type and configuration");
+  const long long items =
+      (long long)(A->M / A->bR) * ((N + nt - 1) / nt) * (run_cfg.split_k > 1 ? run_cfg.split_k : 1);
+  if (items >= (1ll << 30))
     return fail(SPMM_ERR_SCRATCH_TOO_SMALL,
                 "problem has " + std::to_string(items) +
-                    " work items; the allocation-free variant's 32-bit queue holds at most 2^30");
+                    " work items; the allocation-free variant's 32-bit queue holds fewer than 2^30");
 
   unsigned* scratch = nullptr;
   spmm_status st = scratch_for_current_device(&scratch);
   if (st != SPMM_OK) return st;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // Every call shares the array: the error word and the queue pair start at zero.
   SPMM_CUDA_TRY(cudaMemsetAsync(scratch, 0, 3 * sizeof(unsigned), s));
 
@@ -98,10 +115,7 @@ spmm_status spmm_bcsr_mm_noalloc(const spmm_bcsr_desc* A, const spmm_dense_desc*
   r.N = N;
   r.C = C;
   r.ldc = ldc;
-  std::memset(&r.cfg, 0, sizeof(r.cfg));
-  if (cfg) r.cfg = *cfg;
-  r.cfg.kernel = 2;
-  r.cfg.schedule = 1;
+  r.cfg = run_cfg;
   r.stream = s;
   r.err_word = scratch;
   r.queue = scratch + 1;
@@ -109,6 +123,7 @@ spmm_status spmm_bcsr_mm_noalloc(const spmm_bcsr_desc* A, const spmm_dense_desc*
 }
 
 spmm_status spmm_noalloc_error_check(void* stream) {
+  clear_error();
   unsigned* scratch = nullptr;
   spmm_status st = scratch_for_current_device(&scratch);
   if (st != SPMM_OK) return st;

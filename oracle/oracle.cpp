@@ -7,7 +7,7 @@
 // benchmark load it.
 //
 // Pinning: the generator and BCSR restatements below are checked against the
-// reference's own sources built from its tree (oracle/build_ref.sh -> _ref/),
+// reference's own sources built from its tree (oracle/Makefile, `make ref`),
 // and against committed fixtures made from that build (tests/golden/).
 //
 // Reference citations are paths inside hosseinal/MatrixMultiplicationCUDA.
@@ -311,6 +311,134 @@ void oracle_bcsr_matmul_f64(const int* row_ptr, const int* col_idx, const double
         }
     }
   }
+}
+
+// The same product split by block rows over nthreads host threads (each block
+// row's arithmetic is unchanged, so the result equals the one-thread call).
+void oracle_bcsr_matmul_f64_mt(const int* row_ptr, const int* col_idx, const double* vals,
+                               int bR, int bC, const double* B, int N, int br0, int br1,
+                               double* C, int nthreads) {
+  if (nthreads <= 1) {
+    oracle_bcsr_matmul_f64(row_ptr, col_idx, vals, bR, bC, B, N, br0, br1, C);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int n = br1 - br0;
+  for (int t = 0; t < nthreads; ++t) {
+    const int a = br0 + (int)((long long)n * t / nthreads), b = br0 + (int)((long long)n * (t + 1) / nthreads);
+    if (a < b)
+      th.emplace_back([=] {
+        oracle_bcsr_matmul_f64(row_ptr, col_idx, vals, bR, bC, B, N, a, b, C + (size_t)(a - br0) * bR * N);
+      });
+  }
+  for (auto& x : th) x.join();
+}
+
+// ---------------------------------------------------------------------------
+// The synthetic workloads' generators, restated so that a run of the
+// reference's host multiply can build its inputs without the library. The
+// library's definition (bcsr_spmm_host.h, spmm_gen_structure / _values /
+// _dense): every random number is a stateless hash of (seed, stream, index)
+// -- the SplitMix64 finaliser applied twice -- so any block or element can be
+// drawn on its own. Uniform draws take the hash's top 53 bits; normal draws
+// are Box-Muller over two uniform draws 2i and 2i + 1. The tests check these
+// bit for bit against the library's host generators.
+// ---------------------------------------------------------------------------
+namespace {
+uint64_t splitmix_final(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+double draw_u01(uint64_t seed, uint64_t stream, uint64_t index) {
+  const uint64_t key = splitmix_final(seed * 0x2545f4914f6cdd1dull + stream);
+  return (double)(splitmix_final(key ^ index) >> 11) / 9007199254740992.0;
+}
+double draw_normal(uint64_t seed, uint64_t stream, uint64_t index) {
+  const double u1 = std::max(draw_u01(seed, stream, 2 * index), 1e-300);
+  const double u2 = draw_u01(seed, stream, 2 * index + 1);
+  return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+}
+}  // namespace
+
+// Block structure (row_ptr[M/bR + 1], col_idx up to (M/bR)*(K/16) entries).
+// pattern 0: each block independently kept with probability `density`;
+// 1: a band of `param` block columns either side of the block row's diagonal
+//    span, each kept with probability min(1, density*KB / (2*param + bR/16));
+// 2: dense square diagonal tiles of `param` elements;
+// 3: per-row counts round(exp(mu + sigma z)) (log-normal with mean density*KB
+//    and coefficient of variation `param`, clipped to [0, KB]) of distinct
+//    columns drawn by Floyd's method.
+// Returns nnzb, or -1 for bad sizes or an unknown pattern.
+long long oracle_gen_structure(int M, int K, int bR, int pattern, double density, double param,
+                               unsigned long long seed, int* row_ptr, int* col_idx) {
+  if (bR <= 0 || M % bR != 0 || K % 16 != 0 || pattern < 0 || pattern > 3) return -1;
+  const int rows = M / bR, kb = K / 16;
+  long long nnz = 0;
+  row_ptr[0] = 0;
+  std::vector<char> taken;
+  for (int r = 0; r < rows; ++r) {
+    switch (pattern) {
+      case 0:
+        for (int c = 0; c < kb; ++c)
+          if (draw_u01(seed, 1, (uint64_t)r * kb + c) < density) col_idx[nnz++] = c;
+        break;
+      case 1: {
+        const int half = (int)param;
+        const int first = std::max(0, (int)((long long)r * bR / 16) - half);
+        const int last = std::min(kb - 1, (int)(((long long)r * bR + bR - 1) / 16) + half);
+        const double keep = std::min(1.0, density * kb / (2.0 * half + bR / 16.0));
+        for (int c = first; c <= last; ++c)
+          if (keep >= 1.0 || draw_u01(seed, 2, (uint64_t)r * kb + c) < keep) col_idx[nnz++] = c;
+        break;
+      }
+      case 2: {
+        const long long tile = (long long)param;
+        const long long t = (long long)r * bR / tile;
+        for (int c = 0; c < kb; ++c)
+          if ((long long)c * 16 / tile == t) col_idx[nnz++] = c;
+        break;
+      }
+      default: {
+        const double s2 = std::log(1.0 + param * param);
+        const double mu = std::log(std::max(density * kb, 1e-9)) - 0.5 * s2;
+        long long count = std::llround(std::exp(mu + std::sqrt(s2) * draw_normal(seed, 3, (uint64_t)r)));
+        count = std::min<long long>(std::max(count, 0LL), kb);
+        taken.assign(kb, 0);
+        uint64_t n = 0;
+        for (long long top = kb - count; top < kb; ++top) {
+          const long long pick = (long long)(draw_u01(seed, 4, ((uint64_t)r << 32) + n++) * (double)(top + 1));
+          taken[taken[pick] ? top : pick] = 1;
+        }
+        for (int c = 0; c < kb; ++c)
+          if (taken[c]) col_idx[nnz++] = c;
+      }
+    }
+    row_ptr[r + 1] = (int)nnz;
+  }
+  return nnz;
+}
+
+// Block values, nnzb blocks of bR*bC fp32. dist 0: uniform[-1, 1] (stream 5);
+// dist 1: N(0,1) (stream 7) times 10^(6u - 3) per block (u from stream 6);
+// dist 2: N(0,1).
+void oracle_gen_values(long long nnzb, int bR, int bC, int dist, unsigned long long seed, float* out) {
+  const long long per = (long long)bR * bC;
+  for (long long b = 0; b < nnzb; ++b) {
+    const double scale = dist == 1 ? std::pow(10.0, 6.0 * draw_u01(seed, 6, (uint64_t)b) - 3.0) : 1.0;
+    for (long long e = 0; e < per; ++e) {
+      const uint64_t i = (uint64_t)(b * per + e);
+      out[b * per + e] = dist == 0 ? (float)(2.0 * draw_u01(seed, 5, i) - 1.0)
+                                   : (float)(draw_normal(seed, 7, i) * scale);
+    }
+  }
+}
+
+// Dense values: dist 0 uniform[-1, 1] (stream 8), otherwise N(0,1) (stream 9).
+void oracle_gen_dense(long long count, int dist, unsigned long long seed, float* out) {
+  for (long long i = 0; i < count; ++i)
+    out[i] = dist == 0 ? (float)(2.0 * draw_u01(seed, 8, (uint64_t)i) - 1.0) : (float)draw_normal(seed, 9, (uint64_t)i);
 }
 
 // maxdiff / avgrelerr / rmse of miscutil.cpp:35-74, generalised from n x n to a

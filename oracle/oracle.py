@@ -18,9 +18,22 @@ REF_RUNNER = os.path.join(HERE, "libref_wmma.so")
 P = ctypes.c_void_p
 
 
+def reference_tree():
+    """Where the reference's sources are: $MMC_REFERENCE_TREE, else the default
+    that oracle/Makefile holds (the one place that names it)."""
+    env = os.environ.get("MMC_REFERENCE_TREE")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "--no-print-directory", "print-ref"], capture_output=True,
+                       text=True)
+    return r.stdout.strip() or None
+
+
 def build(ref_tree=None):
-    """make liboracle.so (and the WMMA runner); with ref_tree also the _ref build."""
+    """make liboracle.so (and the WMMA runner); where the reference tree is present
+    (ref_tree, else reference_tree()) also the _ref build from its sources."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    ref_tree = ref_tree or reference_tree()
     if ref_tree and os.path.isdir(ref_tree):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref_tree], check=True)
     if os.path.exists(REF_CUBIN):
@@ -50,6 +63,14 @@ def lib():
                                                 ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
         L.oracle_bcsr_matmul_f64.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, P]
+        L.oracle_bcsr_matmul_f64_mt.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
+        L.oracle_gen_structure.restype = ctypes.c_longlong
+        L.oracle_gen_structure.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong, P, P]
+        L.oracle_gen_values.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_ulonglong, P]
+        L.oracle_gen_dense.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_ulonglong, P]
         L.oracle_maxdiff.restype = ctypes.c_float
         L.oracle_maxdiff.argtypes = [P, P, ctypes.c_size_t]
         L.oracle_avgrelerr.restype = ctypes.c_float
@@ -149,8 +170,9 @@ def bcsr_matmul_f32_mt(row_ptr, col_idx, vals_bits, bR, B_f32, br0=0, br1=None, 
     return C
 
 
-def bcsr_matmul_f64(row_ptr, col_idx, vals, bR, bC, B, br0=0, br1=None):
-    """FP64 product of a BCSR A (block values in double) and a dense B (double)."""
+def bcsr_matmul_f64(row_ptr, col_idx, vals, bR, bC, B, br0=0, br1=None, threads=1):
+    """FP64 product of a BCSR A (block values in double) and a dense B (double),
+    block rows [br0, br1), split by block rows over `threads` host threads."""
     rp = np.ascontiguousarray(row_ptr, np.int32)
     ci = np.ascontiguousarray(col_idx, np.int32)
     v = np.ascontiguousarray(vals, np.float64)
@@ -158,8 +180,37 @@ def bcsr_matmul_f64(row_ptr, col_idx, vals, bR, bC, B, br0=0, br1=None):
     N = Bd.shape[1]
     br1 = len(rp) - 1 if br1 is None else br1
     C = np.empty(((br1 - br0) * bR, N), np.float64)
-    lib().oracle_bcsr_matmul_f64(_p(rp), _p(ci), _p(v), bR, bC, _p(Bd), N, br0, br1, _p(C))
+    lib().oracle_bcsr_matmul_f64_mt(_p(rp), _p(ci), _p(v), bR, bC, _p(Bd), N, br0, br1, _p(C), int(threads))
     return C
+
+
+PATTERN_RANDOM, PATTERN_BAND, PATTERN_BLOCKDIAG, PATTERN_LOGNORMAL = 0, 1, 2, 3
+DIST_UNIFORM, DIST_SCALED_NORMAL, DIST_NORMAL = 0, 1, 2
+
+
+def gen_structure(M, K, bR, pattern, density, param=0.0, seed=0):
+    """The synthetic workloads' block structure (row_ptr, col_idx), restated
+    from the library's counter-based generator definition."""
+    rp = np.empty(M // bR + 1, np.int32)
+    ci = np.empty(max((M // bR) * (K // 16), 1), np.int32)
+    n = lib().oracle_gen_structure(M, K, bR, pattern, float(density), float(param), seed, _p(rp), _p(ci))
+    if n < 0:
+        raise ValueError("bad generator arguments")
+    return rp, ci[:n].copy()
+
+
+def gen_values(nnzb, bR, bC, dist, seed):
+    """nnzb blocks of bR*bC fp32 values (flat), restated generator."""
+    out = np.empty(max(nnzb * bR * bC, 1), np.float32)
+    lib().oracle_gen_values(nnzb, bR, bC, dist, seed, _p(out))
+    return out[:nnzb * bR * bC]
+
+
+def gen_dense(rows, cols, dist, seed):
+    """rows x cols fp32 values, restated generator."""
+    out = np.empty((rows, cols), np.float32)
+    lib().oracle_gen_dense(rows * cols, dist, seed, _p(out))
+    return out
 
 
 def maxdiff(A, B):

@@ -174,4 +174,4 @@ def main(ref_tree):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else oracle.reference_tree())

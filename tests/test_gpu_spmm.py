@@ -6,6 +6,8 @@ check, nvbench_main.cu:357-364), and with the FP64 product at a normwise
 relative error <= 1e-5 (max) / 1e-5 (Frobenius) -- the fp16-rounded inputs are
 exact in FP64, so only the fp32 accumulation order differs.
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -133,6 +135,37 @@ def test_variant_launchers_agree(dev):
     m.sparseMatrixMulTensorAdaptive(*args, C2, M, N, 3, K)
     torch.cuda.synchronize()
     assert torch.equal(C1, C2)
+
+
+VARIANTS = {16: ["sparseMatrixMulTensor_v2_launch", "sparseMatrixMulTensor_v3_launch",
+                 "sparseMatrixMulTensor_v1_improved_launch"],
+            32: ["sparseMatrixMulTensor32x16_v2_launch", "sparseMatrixMulTensor32x16_shared_launch",
+                 "sparseMatrixMulTensor32x16_shared_vectorized_launch",
+                 "sparseMatrixMulTensor32x16_v2_shared_vectorized_launch"],
+            64: ["sparseMatrixMulTensor64x16_v2_launch"]}
+PATTERN = {16: "blockrandom", 32: "pattern32by16", 64: "pattern64by16"}
+
+
+@pytest.mark.parametrize("bR", [16, 32, 64])
+def test_named_variant_launchers(dev, bR):
+    """Every variant name the reference declares (src/cuda_kernels.cuh:47-99) has
+    its own C-ABI launcher; each must give the base launcher's result bit for bit
+    (the same pipeline runs), and that result must match the host multiply."""
+    M, K, N = 256, 256, 96
+    A, B, hdr, idx, data = make_problem(M, K, N, PATTERN[bR], 0.7, 16, bR)
+    d = [to_dev(hdr, dev), to_dev(idx, dev), to_dev(data.view(np.float16), dev), to_dev(B.view(np.float16), dev)]
+    base = torch.empty((M, N), device=dev)
+    LAUNCH[bR](*d, base, M, N, K)
+    m.device_error_check()
+    assert float(np.max(np.abs(base.cpu().numpy() - oracle.cpu_matmul_ref(A, B)))) <= 1e-2
+    L = m.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    for name in VARIANTS[bR]:
+        C = torch.full((M, N), float("nan"), device=dev)
+        rc = getattr(L, name)(*[ctypes.c_void_p(x.data_ptr()) for x in d + [C]], M, N, K, ctypes.c_void_p(st))
+        assert rc == 0, (name, m._lib.last_error())
+        m.device_error_check()
+        assert torch.equal(C, base), name
 
 
 @pytest.mark.skipif(not oracle.ref_wmma_available(), reason="reference kernels not built")
