@@ -95,6 +95,7 @@ def build_tools(verbose=False):
         src = os.path.join(HARNESS, f)
         exe = os.path.join(OUT, f[:-3])
         deps = [src, LIB] + [os.path.join(ROOT, "include", h) for h in os.listdir(os.path.join(ROOT, "include"))]
+        deps += [os.path.join(HARNESS, h) for h in os.listdir(HARNESS) if h.endswith((".cuh", ".h"))]
         if not (os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps)):
             cmd = [NVCC] + ARCH + ["-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src, "-o", exe + ".tmp",
                                    "-L" + OUT, "-lbcsr_spmm", "-lcublas", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]

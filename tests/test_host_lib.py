@@ -193,6 +193,20 @@ int main() {
     assert (h_nnzb, h_nnz) == (len(hidx), len(cidx))
 
 
+def test_nvbench_benches_registered():
+    """The NVBench-form benches list every reference bench name with its axes
+    (no GPU needed to list them)."""
+    exe = os.path.join(os.path.dirname(m.lib_path), "spmm_nvbench_benches")
+    r = subprocess.run([exe, "--list"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    names = [line.split()[1] for line in r.stdout.splitlines()]
+    for n in ("sparseMatrixMulTensor", "sparseMatrixMulTensor_v2", "sparseMatrixMulTensor32x16",
+              "sparseMatrixMulTensor32x16_v2_shared_vectorized", "sparseMatrixMulTensor64x16",
+              "sparseMatrixMulTensorAdaptive_16x16", "sparseMatrixMulTensorAdaptive_32x16"):
+        assert n in names
+    assert "PAT=[0,1,2,3,4,5,6]" in r.stdout and "SPARS=[60,70,80,90]" in r.stdout
+
+
 def test_harness_built_and_prints_usage():
     exe = os.path.join(os.path.dirname(m.lib_path), "spmm_nvbench")
     assert os.path.exists(exe)
