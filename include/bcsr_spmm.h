@@ -88,6 +88,13 @@ const char* spmm_last_error(void);
  * written (rows whose block row is empty get zeros), so C need not be cleared.
  * N must be a multiple of 8 and ldb a multiple of 8 (16-byte TMA strides);
  * E4M3 needs multiples of 16. cfg may be NULL.
+ * E4M3 with kernel 0 runs the mma.sync pipeline, which takes any fp32 block
+ * scale. Kernel 2 runs the tcgen05 block-scaled kernels (kind::mxf8f6f4):
+ * every block scale must be a positive normal power of two, as spmm_quantize
+ * makes them (another scale raises a flag spmm_device_error_check reports);
+ * each 16-wide block is a K = 32 MMA whose second half multiplies zeros by
+ * the panel of the next 128 output columns, so a NaN stored in B can reach
+ * the C entry 128 columns to its left in rows whose blocks read that B row.
  */
 spmm_status spmm_bcsr_mm(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N,
                          float* C, int ldc, const spmm_config* cfg, void* stream);
@@ -216,7 +223,8 @@ spmm_status spmm_gpu_generate_matrix(int rows, int cols, double sparsity, const 
 /* ---- precision conversion (device, asynchronous) ------------------------------
  * From fp32 block values (the exact values before storage rounding):
  *   to fp16 / bf16 (round to nearest even),
- *   to e4m3 with one scale per block (scale = max|block| / 448, 1 for all-zero blocks),
+ *   to e4m3 with one scale per block (scale = the smallest power of two >= max|block| / 448,
+ *     1 for all-zero blocks; a power of two is what the tcgen05 e4m3 kernels need),
  *   to an fp16 hi/lo pair (hi = fp16(x), lo = fp16(x - hi)).
  * `count` elements, `block_elems` elements per scale block (E4M3 only). */
 spmm_status spmm_quantize(const float* src, size_t count, spmm_dtype dtype, int block_elems,
@@ -448,7 +456,10 @@ spmm_status spmm_noalloc_error_check(void* stream);
  * when the wait gave up and the kernel exited cleanly (synchronises). */
 spmm_status spmm_debug_wait_timeout(unsigned long long timeout_ns, void* stream);
 /* Synchronises the stream, then reads and clears the device error word that the
- * pipelines set when a bounded wait gives up; SPMM_ERR_TIMEOUT if it was set. */
+ * pipelines set when a bounded wait gives up; SPMM_ERR_TIMEOUT if it was set.
+ * SPMM_ERR_INVALID_ARG when the only flag is the tcgen05 e4m3 kernels' scale
+ * check (a block scale that is not a positive normal power of two; that
+ * product used the scale's exponent alone). */
 spmm_status spmm_device_error_check(void* stream);
 /* Number of SMs of the current device (for grid sizing in callers). */
 int spmm_device_sm_count(void);

@@ -241,12 +241,23 @@ __global__ void k_absmax_small(const float* src, size_t n, int block_elems, floa
   for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) scales[b] = m;
 }
-// max -> scale: max / 448 (the largest finite e4m3), 1 for an all-zero block.
+// max -> scale: the smallest power of two >= max / 448 (448 is the largest
+// finite e4m3), 1 for an all-zero block, kept within the normal fp32 range.
+// A power of two is exact as a UE8M0 scale factor (the tcgen05 e4m3 kernels
+// apply it inside the MMA), and dividing by it is exact; the block's largest
+// value lands in (224, 448], where e4m3 keeps its full 4 significant bits.
 __global__ void k_finish_scales(float* scales, size_t nblocks) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nblocks;
        i += (size_t)gridDim.x * blockDim.x) {
     const float m = scales[i];
-    scales[i] = m > 0.f ? m / 448.0f : 1.0f;
+    float sc = 1.0f;
+    if (m > 0.f) {
+      int e = 0;
+      const float f = frexpf(m / 448.0f, &e);   // m / 448 = f * 2^e, f in [0.5, 1)
+      sc = ldexpf(1.0f, f == 0.5f ? e - 1 : e);
+      sc = fminf(fmaxf(sc, 0x1p-126f), 0x1p127f);
+    }
+    scales[i] = sc;
   }
 }
 __global__ void k_to_e4m3(const float* src, size_t n, int block_elems, const float* scales,

@@ -242,21 +242,25 @@ spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const v
 }
 
 spmm_status encode_panel_map_3d(CUtensorMap* map, const void* base, uint64_t N, uint64_t K,
-                                uint64_t row_stride_bytes, uint32_t boxes) {
-  if (N % 64 || boxes == 0 || boxes > 256) return fail(SPMM_ERR_UNSUPPORTED, "panel map needs N % 64 == 0");
-  const MapKey key = map_key(3, (int)CU_TENSOR_MAP_DATA_TYPE_UINT16, (int)CU_TENSOR_MAP_SWIZZLE_128B, base, 64, K,
-                             N / 64, row_stride_bytes, 128, 64, 16, boxes);
+                                uint64_t row_stride_bytes, uint32_t boxes, int elem_bytes) {
+  if (elem_bytes != 1 && elem_bytes != 2) return fail(SPMM_ERR_UNSUPPORTED, "panel map: 8- or 16-bit elements");
+  const uint64_t W = 128 / (uint64_t)elem_bytes;
+  const CUtensorMapDataType dt = elem_bytes == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+  if (N % W || boxes == 0 || boxes > 256)
+    return fail(SPMM_ERR_UNSUPPORTED, "panel map needs N to be a multiple of 128 bytes of columns");
+  const MapKey key = map_key(3, (int)dt, (int)CU_TENSOR_MAP_SWIZZLE_128B, base, W, K, N / W, row_stride_bytes, 128,
+                             (uint32_t)W, 16, boxes);
   if (map_lookup(key, map)) return SPMM_OK;
   CUtensorMap probe;
-  spmm_status st = encode_tile_map_2d(&probe, CU_TENSOR_MAP_DATA_TYPE_UINT16, base, N, K, row_stride_bytes,
-                                      64, 16, CU_TENSOR_MAP_SWIZZLE_128B);   // resolves the entry point
+  spmm_status st = encode_tile_map_2d(&probe, dt, base, N, K, row_stride_bytes, (uint32_t)W, 16,
+                                      CU_TENSOR_MAP_SWIZZLE_128B);   // resolves the entry point
   if (st != SPMM_OK) return st;
-  cuuint64_t dims[3] = {64, K, N / 64};
+  cuuint64_t dims[3] = {W, K, N / W};
   cuuint64_t strides[2] = {row_stride_bytes, 128};
-  cuuint32_t box[3] = {64, 16, boxes};
+  cuuint32_t box[3] = {(cuuint32_t)W, 16, boxes};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void*>(base), dims, strides, box,
-                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+  CUresult r = g_encode(map, dt, 3, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     return fail(SPMM_ERR_UNSUPPORTED, "3-D panel tensor map rejected (" + std::to_string((int)r) + ")");
@@ -284,8 +288,11 @@ spmm_status spmm_device_error_check(void* stream) {
   SPMM_CUDA_TRY(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
   if (v) {
     SPMM_CUDA_TRY(cudaMemset(w, 0, sizeof(unsigned)));
-    return fail(SPMM_ERR_TIMEOUT, "a device-side pipeline wait timed out (code " +
-                                      std::to_string(v) + ")");
+    if (v == 64u)   // only the scale check fired: every wait completed
+      return fail(SPMM_ERR_INVALID_ARG,
+                  "an e4m3 block scale is not a positive normal power of two (the tcgen05 e4m3 kernels take "
+                  "each scale as a UE8M0 exponent; spmm_quantize makes such scales)");
+    return fail(SPMM_ERR_TIMEOUT, "a device-side pipeline wait timed out (code " + std::to_string(v) + ")");
   }
   return SPMM_OK;
 }
@@ -331,7 +338,9 @@ spmm_status spmm_bcsr_mm(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int 
   if (cfg) r.cfg = *cfg;
   r.stream = static_cast<cudaStream_t>(stream);
   if (r.cfg.kernel == 3) return launch_tc64(r);
-  if (r.cfg.kernel == 2 || (r.cfg.kernel == 0 && A->bR == 64)) {
+  // kernel 0: tcgen05 for 64-row blocks (not e4m3, whose tcgen05 kernels need
+  // power-of-two block scales), mma.sync otherwise
+  if (r.cfg.kernel == 2 || (r.cfg.kernel == 0 && A->bR == 64 && !e4m3)) {
     spmm_status st = launch_tc(r);
     if (st != SPMM_ERR_UNSUPPORTED || r.cfg.kernel == 2) return st;
     g_last_error.clear();

@@ -55,13 +55,14 @@ spmm_status encode_tile_map_2d(CUtensorMap* map, CUtensorMapDataType dt, const v
                                uint64_t inner, uint64_t outer, uint64_t row_stride_bytes,
                                uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz);
 
-// B (K x N, row-major, 16-bit elements) as a 3-D tensor {64 columns, K rows,
-// N/64 column blocks} with 128-byte swizzle and box {64, 16, boxes}: one TMA
-// copy lands a 16-row panel of 64*boxes columns as consecutive 2 KB atoms
-// (the same shared-memory image as `boxes` separate 64-column 2-D copies).
-// Needs N % 64 == 0 so that no box column lies past the end of a row.
+// B (K x N, row-major, 16-bit or 8-bit elements) as a 3-D tensor {W columns,
+// K rows, N/W column blocks}, W = 128 bytes of columns (64 16-bit, 128 8-bit),
+// with 128-byte swizzle and box {W, 16, boxes}: one TMA copy lands a 16-row
+// panel of W*boxes columns as consecutive 2 KB atoms (the same shared-memory
+// image as `boxes` separate W-column 2-D copies). Needs N % W == 0 so that no
+// box column lies past the end of a row.
 spmm_status encode_panel_map_3d(CUtensorMap* map, const void* base, uint64_t N, uint64_t K,
-                                uint64_t row_stride_bytes, uint32_t boxes);
+                                uint64_t row_stride_bytes, uint32_t boxes, int elem_bytes = 2);
 
 struct LaunchRequest {
   const spmm_bcsr_desc* A;

@@ -79,6 +79,13 @@ struct TcParams {
   const int* pair;
   const int* parts;
   unsigned* counters;
+  // e4m3: A's per-block scales (powers of two; each block's UE8M0 scale factor
+  // is its exponent), B's scale (applied in the epilogue) and K (a partial
+  // group's spare panel slot is filled by a copy from row K, past the end of B,
+  // which reads zeros)
+  const float* scales;
+  float b_scale;
+  int K;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* ptr) {
@@ -99,28 +106,64 @@ __device__ __forceinline__ void st_release_gpu(unsigned* ptr, unsigned v) {
 // their G B panels, and one mbarrier pair tracks it. (An mbarrier wait in the
 // thread that issues UMMAs costs ~200 cycles once UMMAs are in flight, so the
 // MMA thread waits and commits once per group, not once per block.)
+//
+// E4M3 (MODE_E4M3) runs the same pipeline on the block-scaled MMA
+// (kind::mxf8f6f4, K = 32, one UE8M0 scale factor per row and column for the
+// 32-element K block). A block is 16 wide, so each block is one K = 32 MMA
+// whose second K half is zero on the A side (the block descriptor's
+// K-direction core-matrix stride points at a zeroed region after the group's
+// blocks) and, on the panel side, reads the next 2 KB of the slot: the next
+// 128-column slice, or a zero-filled panel slot / tail. A's per-block scale
+// (a power of two) becomes the MMA's B-side scale factor: a 512-byte tile of
+// its UE8M0 byte, written by B issuer 0 into the ring slot and moved to TMEM
+// with tcgen05.cp right before the block's MMAs. Every byte of the tile is the
+// same, so the factor does not depend on which TMEM cells the MMA reads. The
+// panel side's factor is a constant 1 (0x7F), copied once per CTA. B's scale
+// multiplies C in the epilogue.
 template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
 struct TcCfg {
   static constexpr bool kSplit = MODE == MODE_SPLIT;
+  static constexpr bool kE4 = MODE == MODE_E4M3;
   static constexpr int kParts = kSplit ? 2 : 1;
   static constexpr int kJ = NT / 128;                 // 128-column MMA slices per item
-  static constexpr int kBoxBytes = 16 * 128;          // 16 rows x 64 fp16 columns
-  static constexpr int kPanelBytes = (NT / 64) * kBoxBytes;
-  static constexpr int kABytes = BR * 32;             // bR rows x 16 fp16
+  static constexpr int kBoxBytes = 16 * 128;          // 16 rows x 128 bytes: 64 fp16 or 128 e4m3 columns
+  static constexpr int kBoxCols = kE4 ? 128 : 64;
+  static constexpr int kPanelBytes = (NT / kBoxCols) * kBoxBytes;
+  static constexpr int kSliceBytes = kPanelBytes / kJ;   // one 128-column slice of a panel
+  static constexpr int kABytes = BR * (kE4 ? 16 : 32);   // bR rows x 16 elements
   static constexpr int kAPart = G * kABytes;          // one part (hi or lo) of a group's A blocks
-  static constexpr int kAStage = ((kAPart * kParts + 1023) / 1024) * 1024;
-  static constexpr int kStage = kAStage + G * kPanelBytes * kParts;
+  // fp16 / bf16 / split slot: [A (hi, lo) | B panels (hi, lo)]
+  // e4m3 slot: [A blocks | zeros (one block) | scale tiles | B panels | 2 KB zero tail]
+  static constexpr int kAZeroOff = kAPart;
+  static constexpr int kScaleOff = kAZeroOff + kABytes;
+  static constexpr int kAStage = kE4 ? ((kScaleOff + G * 512 + 1023) / 1024) * 1024
+                                     : ((kAPart * kParts + 1023) / 1024) * 1024;
+  static constexpr int kTailOff = kAStage + G * kPanelBytes * kParts;
+  static constexpr int kStage = kE4 ? ((kTailOff + 2048 + 1023) / 1024) * 1024 : kTailOff;
+  // e4m3, after the ring: the panel-side scale tile (512 bytes of 0x7F)
+  static constexpr int kExtra = kE4 ? 512 : 0;
   static constexpr int kAccCols = kJ * BR;            // TMEM columns of one accumulator
-  static constexpr int kTmemCols = (ACC * kAccCols) < 32 ? 32 : ACC * kAccCols;
-  static constexpr size_t kSmem = 1024 + (size_t)STAGES * kStage + 1024;
-  static_assert((kTmemCols & (kTmemCols - 1)) == 0 && kTmemCols <= 512, "TMEM columns");
+  // e4m3 scale factors in TMEM: 4 columns for the panel side, 4 per block of the ring
+  static constexpr int kSfaCol = ACC * kAccCols;
+  static constexpr int kSfbCol = kSfaCol + 4;
+  static constexpr int kUsedCols = kE4 ? kSfbCol + 4 * STAGES * G : ACC * kAccCols;
+  static constexpr int kTmemCols = kUsedCols <= 32 ? 32 : kUsedCols <= 64 ? 64 : kUsedCols <= 128 ? 128
+                                   : kUsedCols <= 256 ? 256 : 512;
+  static constexpr size_t kSmem = 1024 + (size_t)STAGES * kStage + kExtra + 1024;
+  static_assert(kUsedCols <= 512, "TMEM columns");
   static_assert(NT % 128 == 0, "NT");
   static_assert(G * BR <= 256 && 32 % G == 0, "a group is one TMA box and never straddles an index chunk");
+  static_assert(!kE4 || G <= 4, "e4m3: a partial group's spare slot is copied by the B issuer of that slot");
   // kind::f16 instruction descriptor: D f32, A/B f16 or bf16, A MN-major, B K-major,
   // N = BR, M = 128.
-  static constexpr uint32_t kIdesc = (1u << 4) | ((MODE == MODE_BF16 ? 1u : 0u) << 7) |
-                                     ((MODE == MODE_BF16 ? 1u : 0u) << 10) | (1u << 15) |
-                                     ((uint32_t)(BR >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  static constexpr uint32_t kIdescF16 = (1u << 4) | ((MODE == MODE_BF16 ? 1u : 0u) << 7) |
+                                        ((MODE == MODE_BF16 ? 1u : 0u) << 10) | (1u << 15) |
+                                        ((uint32_t)(BR >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  // kind::mxf8f6f4 block-scaled descriptor: A and B e4m3 (format 0), A MN-major,
+  // B K-major, N = BR, UE8M0 scale factors, M = 128, scale-factor ids 0.
+  static constexpr uint32_t kIdescE4 =
+      (1u << 15) | ((uint32_t)(BR >> 3) << 17) | (1u << 23) | ((uint32_t)(128 >> 4) << 24);
+  static constexpr uint32_t kIdesc = kE4 ? kIdescE4 : kIdescF16;
 };
 
 constexpr int kTcThreads = 320;   // 10 warps
@@ -137,7 +180,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)STAGES * Cfg::kStage);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)STAGES * Cfg::kStage + Cfg::kExtra);
   // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done, qfull[kQ], qempty[kQ];
   // then the TMEM address and the item ring
   const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES;
@@ -150,7 +193,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 32) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(full0 + 8 * s, 1);            // the lead's arrive (it expects the whole group's bytes)
+      // the lead's arrive (it expects the whole group's bytes); e4m3 also B
+      // issuer 0's, after it has written the group's scale tiles
+      mbar_init(full0 + 8 * s, Cfg::kE4 ? 2 : 1);
       mbar_init(empty0 + 8 * s, 1);           // the MMA thread's commit
     }
     for (int b = 0; b < 2; ++b) {
@@ -177,6 +222,24 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   // stream; everything the caller passes is read after it.
   int4 first = make_int4(0, 0, 0, 0);
   if (warp == 0 && lane == 0 && p.items) first = __ldg(p.items + blockIdx.x);
+  if constexpr (Cfg::kE4) {
+    // Zero each slot's A-side zero block and panel tail (never written by a
+    // copy), fill the panel-side scale tile with UE8M0 1.0, and make the
+    // stores visible to the tensor core's operand reads.
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = threadIdx.x; i < STAGES * (Cfg::kABytes / 16); i += kTcThreads) {
+      const int s = i / (Cfg::kABytes / 16), c = i % (Cfg::kABytes / 16);
+      *reinterpret_cast<uint4*>(smem + (size_t)s * Cfg::kStage + Cfg::kAZeroOff + 16 * c) = z;
+    }
+    for (int i = threadIdx.x; i < STAGES * (2048 / 16); i += kTcThreads) {
+      const int s = i / (2048 / 16), c = i % (2048 / 16);
+      *reinterpret_cast<uint4*>(smem + (size_t)s * Cfg::kStage + Cfg::kTailOff + 16 * c) = z;
+    }
+    if (threadIdx.x < 32)
+      *reinterpret_cast<uint4*>(smem + (size_t)STAGES * Cfg::kStage + 16 * threadIdx.x) =
+          make_uint4(0x7F7F7F7Fu, 0x7F7F7F7Fu, 0x7F7F7F7Fu, 0x7F7F7F7Fu);
+    fence_proxy_async_smem();
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -329,7 +392,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             break;
           }
           const uint32_t fb = full0 + 8 * s;
-          mbar_arrive_expect_tx(fb, (uint32_t)(n * (Cfg::kABytes + Cfg::kPanelBytes) * Cfg::kParts));
+          // e4m3: a partial group also fills panel slot n (zeros), which the
+          // last block's last slice reads as its K padding
+          const int panels = (Cfg::kE4 && n < G) ? n + 1 : n;
+          mbar_arrive_expect_tx(fb, (uint32_t)((n * Cfg::kABytes + panels * Cfg::kPanelBytes) * Cfg::kParts));
           uint8_t* a_dst = smem + (size_t)s * Cfg::kStage;
           const int y0 = j0 * BR;
           if (n == G) {
@@ -394,20 +460,32 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       nt = __shfl_sync(0xffffffffu, nt, 0);
       if (!ok || item < 0) break;
       int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
+      // e4m3, issuer 0: the blocks' scales, staged like the column indices
+      float mysc = 1.f;
+      if constexpr (Cfg::kE4) {
+        if (bidx == 0) mysc = lane < end - start ? __ldg(p.scales + start + lane) : 1.f;
+      }
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
         const int cur = mycol;
+        const float cursc = mysc;
         if (base + 32 < end) mycol = lane < end - base - 32 ? __ldg(p.col_idx + base + 32 + lane) : 0;
+        if constexpr (Cfg::kE4) {
+          if (bidx == 0 && base + 32 < end) mysc = lane < end - base - 32 ? __ldg(p.scales + base + 32 + lane) : 1.f;
+        }
         for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
           const int n = min(G, cnt - i0);
+          // e4m3: a partial group also fills the next panel slot with zeros
+          // (the last block's last slice reads it as K padding)
+          const int nslots = (Cfg::kE4 && n < G) ? n + 1 : n;
           const int s = (int)(gs % STAGES);
           // Wait for the slot only in groups this issuer copies into: such a
           // group cannot be released without its bytes, so the slot's empty
           // barrier is at most one phase ahead. (An issuer that also waited in
           // groups it has no block in could fall two phases behind and miss a
-          // parity flip.)
+          // parity flip.) Issuer 0 copies into every group.
           int bad = 0;
-          if (lane == 0 && bidx < n && gs >= (uint32_t)STAGES &&
+          if (lane == 0 && bidx < nslots && gs >= (uint32_t)STAGES &&
               !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
             atomicOr(p.err, 4u);
             bad = 1;
@@ -415,9 +493,27 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           failed = __shfl_sync(0xffffffffu, bad, 0);
           if (failed) break;
           uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
-          for (int b = bidx; b < n; b += kBIssuers) {
-            const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
-            if constexpr (!Cfg::kSplit) {
+          if constexpr (Cfg::kE4) {
+            if (bidx == 0) {
+              // One 512-byte tile per block, every byte the block scale's
+              // UE8M0 encoding: the exponent field of a power-of-two fp32
+              // (bit 64 of the error word flags a scale that is not one).
+              uint8_t* tiles = smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff;
+              for (int b = 0; b < n; ++b) {
+                const uint32_t bits = __float_as_uint(__shfl_sync(0xffffffffu, cursc, i0 + b));
+                const uint32_t e = (bits >> 23) & 0xFFu;
+                if (lane == 0 && ((bits & 0x807FFFFFu) != 0u || e == 0u || e == 0xFFu)) atomicOr(p.err, 64u);
+                const uint32_t w = e * 0x01010101u;
+                *reinterpret_cast<uint4*>(tiles + b * 512 + 16 * lane) = make_uint4(w, w, w, w);
+              }
+              fence_proxy_async_smem();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(full0 + 8 * s);
+            }
+          }
+          for (int b = bidx; b < nslots; b += kBIssuers) {
+            const int col = __shfl_sync(0xffffffffu, cur, min(i0 + b, 31));
+            if constexpr (!Cfg::kSplit && !Cfg::kE4) {
               if (col < 0 && p.gather_rows) {
                 // Gather block: its panel is 16 arbitrary B rows. Lane L < 4 * (NT / 64)
                 // copies rows 4q .. 4q + 3 (q = L % 4) of 64-column box L / 4 with one
@@ -442,17 +538,21 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             if (lane == 0) {
               const uint32_t fb = full0 + 8 * s;
               uint8_t* b_dst = b_dst0 + (size_t)b * Cfg::kPanelBytes * Cfg::kParts;
+              // the spare slot of a partial e4m3 group is copied from row K:
+              // every row of the box lies past the end of B and reads zeros
+              const int y = (Cfg::kE4 && b >= n) ? p.K : col * 16;
               if (p.panel3d) {
-                tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, col * 16, nt * (NT / 64), fb, pol_b);
+                tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, y, nt * (NT / Cfg::kBoxCols), fb, pol_b);
                 if (Cfg::kSplit)
-                  tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, col * 16, nt * (NT / 64), fb, pol_b);
+                  tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, y, nt * (NT / 64), fb, pol_b);
               } else {
 #pragma unroll
-                for (int bx = 0; bx < NT / 64; ++bx) {
-                  tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), &tmB, nt * NT + bx * 64, col * 16, fb, pol_b);
+                for (int bx = 0; bx < NT / Cfg::kBoxCols; ++bx) {
+                  tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), &tmB, nt * NT + bx * Cfg::kBoxCols, y, fb,
+                                  pol_b);
                   if (Cfg::kSplit)
                     tma_tile_2d_g2s(smem_u32(b_dst + Cfg::kPanelBytes + bx * Cfg::kBoxBytes), &tmBlo,
-                                    nt * NT + bx * 64, col * 16, fb, pol_b);
+                                    nt * NT + bx * 64, y, fb, pol_b);
                 }
               }
             }
@@ -465,6 +565,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     if (lane == 0) {
       uint32_t gs = 0, it = 0;
       bool failed = false;
+      if constexpr (Cfg::kE4)   // the panel side's scale factors: 1.0 for every row
+        tmem_cp_32x128b_x4(tmem + Cfg::kSfaCol,
+                           smem_desc(smem_u32(smem + (size_t)STAGES * Cfg::kStage), 128, 128, kLayoutNone));
       for (;; ++it) {
         int item, start, end;
         if (!read_item(it, &item, &start, &end, 8u) || item < 0) break;
@@ -488,8 +591,23 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           const uint32_t b_slot = a_slot + Cfg::kAStage;
           for (int b = 0; b < n; ++b) {
             const uint32_t b_addr = b_slot + b * Cfg::kPanelBytes * Cfg::kParts;
-            const uint64_t blk_hi = smem_desc(a_slot + b * Cfg::kABytes, 16, 256, kLayoutSW32);
             const uint32_t accum = (j0 + b != start) ? 1u : 0u;
+            if constexpr (Cfg::kE4) {
+              // the block's scale factor into its TMEM columns, then one K = 32
+              // MMA per slice: K 0..15 the block (K-major, no swizzle, 8-row
+              // core matrices 128 bytes apart), K 16..31 the slot's zero block
+              const uint32_t sfb = tmem + Cfg::kSfbCol + (uint32_t)((s * G + b) * 4);
+              tmem_cp_32x128b_x4(sfb, smem_desc(a_slot + Cfg::kScaleOff + b * 512, 128, 128, kLayoutNone));
+              const uint32_t blk = a_slot + b * Cfg::kABytes;
+              const uint64_t blk_d = smem_desc(blk, a_slot + Cfg::kAZeroOff - blk, 128, kLayoutNone);
+#pragma unroll
+              for (int j = 0; j < Cfg::kJ; ++j) {
+                const uint64_t pan = smem_desc(b_addr + j * Cfg::kSliceBytes, 1024, 1024, kLayoutSW128);
+                umma_mxf8_scaled(d0 + j * BR, pan, blk_d, Cfg::kIdesc, tmem + Cfg::kSfaCol, sfb, accum);
+              }
+              continue;
+            }
+            const uint64_t blk_hi = smem_desc(a_slot + b * Cfg::kABytes, 16, 256, kLayoutSW32);
 #pragma unroll
             for (int j = 0; j < Cfg::kJ; ++j) {
               const uint64_t pan_hi = smem_desc(b_addr + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
@@ -601,6 +719,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             float v[16];
             if (!empty) {
               tmem_ld16(taddr + c0, v);
+              if constexpr (Cfg::kE4) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] *= p.b_scale;
+              }
             } else {
 #pragma unroll
               for (int i = 0; i < 16; ++i) v[i] = 0.f;
@@ -687,10 +809,17 @@ const TcEntry kTcEntries[] = {
     SPMM_TC_ENTRY(64, 256, 2, MODE_SPLIT, 2, 2),
     SPMM_TC_ENTRY(64, 128, 3, MODE_SPLIT, 2, 2),
     SPMM_TC_ENTRY(64, 512, 2, MODE_SPLIT, 1, 1),
+    // e4m3: TMEM holds the accumulators and the scale factors (4 columns per
+    // block of the ring), so the 512-column tile and two 256-column
+    // accumulators run one CTA per SM
+    SPMM_TC_ENTRY(64, 256, 6, MODE_E4M3, 1, 2), SPMM_TC_ENTRY(64, 512, 6, MODE_E4M3, 1, 2),
+    SPMM_TC_ENTRY(64, 256, 8, MODE_E4M3, 2, 2), SPMM_TC_ENTRY(64, 128, 8, MODE_E4M3, 2, 2),
+    SPMM_TC_ENTRY(32, 256, 3, MODE_E4M3, 1, 4), SPMM_TC_ENTRY(16, 256, 3, MODE_E4M3, 2, 4),
 };
 
 int tc_mode(spmm_dtype d) {
-  return d == SPMM_F16 ? MODE_F16 : d == SPMM_BF16 ? MODE_BF16 : d == SPMM_F16_SPLIT ? MODE_SPLIT : -1;
+  return d == SPMM_F16 ? MODE_F16 : d == SPMM_BF16 ? MODE_BF16 : d == SPMM_F16_SPLIT ? MODE_SPLIT
+         : d == SPMM_E4M3 ? MODE_E4M3 : -1;
 }
 
 // The instantiation a request runs on (NULL if none): column tile (default 128
@@ -737,7 +866,11 @@ spmm_status launch_tc(const LaunchRequest& r) {
   const spmm_bcsr_desc& A = *r.A;
   const spmm_dense_desc& B = *r.B;
   const int mode = tc_mode(A.dtype);
-  if (mode < 0) return fail(SPMM_ERR_UNSUPPORTED, "tcgen05 pipeline: fp16, bf16 and split fp16 only");
+  if (mode < 0) return fail(SPMM_ERR_UNSUPPORTED, "tcgen05 pipeline: fp16, bf16, split fp16 and e4m3 only");
+  const bool e4 = mode == MODE_E4M3;
+  if (e4 && (r.csr || r.gather_rows))
+    return fail(SPMM_ERR_UNSUPPORTED, "the hybrid product and gather blocks run in fp16 / bf16");
+  if (e4 && !A.scales) return fail(SPMM_ERR_INVALID_ARG, "E4M3 needs per-block scales");
   int nt = 0;
   const TcEntry* e = find_tc(A.bR, mode, r.N, r.cfg, &nt);
   if (!e)
@@ -753,21 +886,27 @@ spmm_status launch_tc(const LaunchRequest& r) {
   if (rows_bound >= (1ull << 31)) return fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline");
   CUtensorMap tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo;
   const void* vals = A.vals ? A.vals : B.data;   // no stored blocks: never dereferenced
-  spmm_status st = encode_tile_map_2d(&tmA1, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals, 16, rows_bound, 32, 16,
-                                      (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
+  // A's values as a [rows x 16] matrix: 16-bit with 32-byte swizzle (the UMMA
+  // K-major SW32 layout), or e4m3 bytes unswizzled (K-major, 8 x 16-byte core
+  // matrices, contiguous per block)
+  const CUtensorMapDataType adt = e4 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+  const CUtensorMapSwizzle aswz = e4 ? CU_TENSOR_MAP_SWIZZLE_NONE : CU_TENSOR_MAP_SWIZZLE_32B;
+  const uint64_t arow = e4 ? 16 : 32;
+  spmm_status st = encode_tile_map_2d(&tmA1, adt, vals, 16, rows_bound, arow, 16, (uint32_t)A.bR, aswz);
   if (st != SPMM_OK) return st;
-  st = encode_tile_map_2d(&tmAg, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals, 16, rows_bound, 32, 16,
-                          (uint32_t)(e->group * A.bR), CU_TENSOR_MAP_SWIZZLE_32B);
+  st = encode_tile_map_2d(&tmAg, adt, vals, 16, rows_bound, arow, 16, (uint32_t)(e->group * A.bR), aswz);
   if (st != SPMM_OK) return st;
-  // B panels: one 3-D copy per panel when N is a multiple of 64, else one 2-D
-  // copy per 64-column box.
-  int panel3d = (r.N % 64 == 0) ? 1 : 0;
-  if (panel3d && encode_panel_map_3d(&tmB, B.data, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * 2,
-                                     (uint32_t)(nt / 64)) != SPMM_OK)
+  // B panels: one 3-D copy per panel when N is a multiple of the 128-byte box
+  // width (64 16-bit or 128 e4m3 columns), else one 2-D copy per box.
+  const int esz = e4 ? 1 : 2, box_cols = 128 / esz;
+  int panel3d = (r.N % box_cols == 0) ? 1 : 0;
+  if (panel3d && encode_panel_map_3d(&tmB, B.data, (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * esz,
+                                     (uint32_t)(nt / box_cols), esz) != SPMM_OK)
     panel3d = 0;
   if (!panel3d) {
-    st = encode_tile_map_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data, (uint64_t)r.N, (uint64_t)A.K,
-                            (uint64_t)B.ldb * 2, 64, 16, CU_TENSOR_MAP_SWIZZLE_128B);
+    st = encode_tile_map_2d(&tmB, e4 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, B.data,
+                            (uint64_t)r.N, (uint64_t)A.K, (uint64_t)B.ldb * esz, (uint32_t)box_cols, 16,
+                            CU_TENSOR_MAP_SWIZZLE_128B);
     if (st != SPMM_OK) return st;
   }
   tmAlo1 = tmA1;
@@ -823,6 +962,9 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.pair = r.pair;
   p.parts = r.parts;
   p.counters = r.counters;
+  p.scales = A.scales;
+  p.b_scale = e4 ? B.scale : 1.0f;
+  p.K = A.K;
   if (r.items) {
     if (p.split > 1 || r.csr || r.gather_rows || (p.queue && !r.queue))
       return fail(SPMM_ERR_UNSUPPORTED, "a planned product runs without split-K, CSR part or shared work queue");

@@ -83,7 +83,9 @@ spmm_status spmm_default_config(int bR, spmm_dtype dtype, int N, spmm_config* ou
   // spmm_bcsr_mm with no configuration: the tcgen05 pipeline for 64-row
   // blocks where it has a kernel (its first instantiation for the column tile:
   // two accumulators, static schedule), else the mma.sync pipeline (depth 4).
-  if (bR == 64 && tc_supported(bR, dtype, N, c)) {
+  // E4M3 stays on mma.sync, which takes any fp32 block scale (the tcgen05
+  // e4m3 kernels need powers of two).
+  if (bR == 64 && dtype != SPMM_E4M3 && tc_supported(bR, dtype, N, c)) {
     c.kernel = 2;
     c.n_tile = N <= 128 ? 128 : 256;
     c.acc_buffers = 2;

@@ -63,8 +63,13 @@ def test_quantize_e4m3_scales(dev):
     x = torch.tensor([[0.0] * 16, [1.0] * 15 + [-448.0 * 3]], device=dev).reshape(-1)
     q, lo, sc = m.quantize(x, m.DType.E4M3, block_elems=16)
     torch.cuda.synchronize()
-    assert sc.cpu().tolist() == [1.0, 3.0]
-    assert q.cpu().numpy()[31] == 0xFE  # -448 in e4m3
+    # the smallest power of two >= max / 448: 1344 / 448 = 3 -> 4
+    assert sc.cpu().tolist() == [1.0, 4.0]
+    assert q.cpu().numpy()[31] == torch.tensor([-336.0]).to(torch.float8_e4m3fn).view(torch.uint8).item()
+    y = torch.tensor([448.0, 0.5, -300.0, 1e-3, 448.0 * 2 ** 20, 3e-38, 2.0 ** -20 * 448, 7.0], device=dev)
+    _, _, sc = m.quantize(y, m.DType.E4M3, block_elems=1)
+    want = [1.0, 2.0 ** -9, 1.0, 2.0 ** -18, 2.0 ** 20, 2.0 ** -126, 2.0 ** -20, 2.0 ** -6]
+    assert sc.cpu().tolist() == want
 
 
 @pytest.mark.parametrize("count,offset", [(4096, 0), (4099, 0), (1003, 1), (257, 3), (3, 0)])
@@ -92,4 +97,4 @@ def test_quantize_single_large_scale_block(dev):
     x = torch.randn(3_000_001, device=dev)
     x[1_234_567] = -99.5
     _, _, sc = m.quantize(x, m.DType.E4M3, block_elems=x.numel())
-    assert sc.numel() == 1 and float(sc[0]) == pytest.approx(99.5 / 448.0, rel=1e-7)
+    assert sc.numel() == 1 and float(sc[0]) == 0.25     # 99.5 / 448 = 0.222 -> 2^-2
