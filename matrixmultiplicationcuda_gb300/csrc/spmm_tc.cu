@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   using Cfg = TcCfg<BR, NT, STAGES, MODE, ACC, G>;
   constexpr int kQ = 4;                       // item hand-off ring depth
   constexpr int kBIssuers = 4;
+  constexpr int kScaleWriter = 3;             // e4m3: the B issuer that writes the scale tiles
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
@@ -460,10 +461,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       nt = __shfl_sync(0xffffffffu, nt, 0);
       if (!ok || item < 0) break;
       int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
-      // e4m3, issuer 0: the blocks' scales, staged like the column indices
+      // e4m3, the scale writer (issuer 3): the blocks' scales, staged like the column indices
       float mysc = 1.f;
       if constexpr (Cfg::kE4) {
-        if (bidx == 0) mysc = lane < end - start ? __ldg(p.scales + start + lane) : 1.f;
+        if (bidx == kScaleWriter) mysc = lane < end - start ? __ldg(p.scales + start + lane) : 1.f;
       }
       for (int base = start; base < end && !failed; base += 32) {
         const int cnt = min(32, end - base);
@@ -471,7 +472,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const float cursc = mysc;
         if (base + 32 < end) mycol = lane < end - base - 32 ? __ldg(p.col_idx + base + 32 + lane) : 0;
         if constexpr (Cfg::kE4) {
-          if (bidx == 0 && base + 32 < end) mysc = lane < end - base - 32 ? __ldg(p.scales + base + 32 + lane) : 1.f;
+          if (bidx == kScaleWriter && base + 32 < end)
+            mysc = lane < end - base - 32 ? __ldg(p.scales + base + 32 + lane) : 1.f;
         }
         for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
           const int n = min(G, cnt - i0);
@@ -483,9 +485,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           // group cannot be released without its bytes, so the slot's empty
           // barrier is at most one phase ahead. (An issuer that also waited in
           // groups it has no block in could fall two phases behind and miss a
-          // parity flip.) Issuer 0 copies into every group.
+          // parity flip.) Issuer 0 copies into every group, and so does the
+          // e4m3 scale writer (its arrival is part of every group's full barrier).
+          const bool writes = bidx < nslots || (Cfg::kE4 && bidx == kScaleWriter);
           int bad = 0;
-          if (lane == 0 && bidx < nslots && gs >= (uint32_t)STAGES &&
+          if (lane == 0 && writes && gs >= (uint32_t)STAGES &&
               !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
             atomicOr(p.err, 4u);
             bad = 1;
@@ -493,24 +497,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           failed = __shfl_sync(0xffffffffu, bad, 0);
           if (failed) break;
           uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
-          if constexpr (Cfg::kE4) {
-            if (bidx == 0) {
-              // One 512-byte tile per block, every byte the block scale's
-              // UE8M0 encoding: the exponent field of a power-of-two fp32
-              // (bit 64 of the error word flags a scale that is not one).
-              uint8_t* tiles = smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff;
-              for (int b = 0; b < n; ++b) {
-                const uint32_t bits = __float_as_uint(__shfl_sync(0xffffffffu, cursc, i0 + b));
-                const uint32_t e = (bits >> 23) & 0xFFu;
-                if (lane == 0 && ((bits & 0x807FFFFFu) != 0u || e == 0u || e == 0xFFu)) atomicOr(p.err, 64u);
-                const uint32_t w = e * 0x01010101u;
-                *reinterpret_cast<uint4*>(tiles + b * 512 + 16 * lane) = make_uint4(w, w, w, w);
-              }
-              fence_proxy_async_smem();
-              __syncwarp();
-              if (lane == 0) mbar_arrive(full0 + 8 * s);
-            }
-          }
           for (int b = bidx; b < nslots; b += kBIssuers) {
             const int col = __shfl_sync(0xffffffffu, cur, min(i0 + b, 31));
             if constexpr (!Cfg::kSplit && !Cfg::kE4) {
@@ -557,6 +543,27 @@ __global__ void __launch_bounds__(kTcThreads, 2)
               }
             }
           }
+          if constexpr (Cfg::kE4) {
+            if (bidx == kScaleWriter) {
+              // After its own copies are in flight: one 512-byte tile per
+              // block, every byte the block scale's UE8M0 encoding, the
+              // exponent field of a power-of-two fp32 (bit 64 of the error
+              // word flags a scale that is not one); then the proxy fence that
+              // makes the tiles visible to tcgen05.cp, and the arrival the
+              // group's full barrier waits for.
+              uint8_t* tiles = smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff;
+              for (int b = 0; b < n; ++b) {
+                const uint32_t bits = __float_as_uint(__shfl_sync(0xffffffffu, cursc, i0 + b));
+                const uint32_t e = (bits >> 23) & 0xFFu;
+                if (lane == 0 && ((bits & 0x807FFFFFu) != 0u || e == 0u || e == 0xFFu)) atomicOr(p.err, 64u);
+                const uint32_t w = e * 0x01010101u;
+                *reinterpret_cast<uint4*>(tiles + b * 512 + 16 * lane) = make_uint4(w, w, w, w);
+              }
+              fence_proxy_async_smem();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(full0 + 8 * s);
+            }
+          }
         }
       }
     }
@@ -589,15 +596,20 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           tc_fence_after();
           const uint32_t a_slot = smem_u32(smem + (size_t)s * Cfg::kStage);
           const uint32_t b_slot = a_slot + Cfg::kAStage;
+          if constexpr (Cfg::kE4) {
+            // the group's scale factors into their TMEM columns, ahead of its MMAs
+            for (int b = 0; b < n; ++b)
+              tmem_cp_32x128b_x4(tmem + Cfg::kSfbCol + (uint32_t)((s * G + b) * 4),
+                                 smem_desc(a_slot + Cfg::kScaleOff + b * 512, 128, 128, kLayoutNone));
+          }
           for (int b = 0; b < n; ++b) {
             const uint32_t b_addr = b_slot + b * Cfg::kPanelBytes * Cfg::kParts;
             const uint32_t accum = (j0 + b != start) ? 1u : 0u;
             if constexpr (Cfg::kE4) {
-              // the block's scale factor into its TMEM columns, then one K = 32
-              // MMA per slice: K 0..15 the block (K-major, no swizzle, 8-row
-              // core matrices 128 bytes apart), K 16..31 the slot's zero block
+              // one K = 32 MMA per slice: K 0..15 the block (K-major, no
+              // swizzle, 8-row core matrices 128 bytes apart), K 16..31 the
+              // slot's zero block; the block's scale factor from its columns
               const uint32_t sfb = tmem + Cfg::kSfbCol + (uint32_t)((s * G + b) * 4);
-              tmem_cp_32x128b_x4(sfb, smem_desc(a_slot + Cfg::kScaleOff + b * 512, 128, 128, kLayoutNone));
               const uint32_t blk = a_slot + b * Cfg::kABytes;
               const uint64_t blk_d = smem_desc(blk, a_slot + Cfg::kAZeroOff - blk, 128, kLayoutNone);
 #pragma unroll
@@ -812,8 +824,9 @@ const TcEntry kTcEntries[] = {
     // e4m3: TMEM holds the accumulators and the scale factors (4 columns per
     // block of the ring), so the 512-column tile and two 256-column
     // accumulators run one CTA per SM
-    SPMM_TC_ENTRY(64, 256, 6, MODE_E4M3, 1, 2), SPMM_TC_ENTRY(64, 512, 6, MODE_E4M3, 1, 2),
+    SPMM_TC_ENTRY(64, 256, 7, MODE_E4M3, 1, 2), SPMM_TC_ENTRY(64, 512, 9, MODE_E4M3, 1, 2),
     SPMM_TC_ENTRY(64, 256, 8, MODE_E4M3, 2, 2), SPMM_TC_ENTRY(64, 128, 8, MODE_E4M3, 2, 2),
+    SPMM_TC_ENTRY(64, 256, 4, MODE_E4M3, 1, 4), SPMM_TC_ENTRY(64, 512, 4, MODE_E4M3, 1, 4),
     SPMM_TC_ENTRY(32, 256, 3, MODE_E4M3, 1, 4), SPMM_TC_ENTRY(16, 256, 3, MODE_E4M3, 2, 4),
 };
 
