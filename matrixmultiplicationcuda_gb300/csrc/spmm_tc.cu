@@ -46,6 +46,7 @@ namespace {
 struct TcParams {
   const int* row_ptr;
   const int* col_idx;
+  const uint8_t* avals;   // A's values (bytes), for the e4m3 bulk copies
   float* C;
   long long ldc;
   int N;
@@ -399,7 +400,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           mbar_arrive_expect_tx(fb, (uint32_t)((n * Cfg::kABytes + panels * Cfg::kPanelBytes) * Cfg::kParts));
           uint8_t* a_dst = smem + (size_t)s * Cfg::kStage;
           const int y0 = j0 * BR;
-          if (n == G) {
+          if constexpr (Cfg::kE4) {
+            // unswizzled e4m3 blocks: the group's n blocks are contiguous in
+            // memory and in the slot, one bulk copy
+            tma_bulk_g2s(smem_u32(a_dst), p.avals + (size_t)j0 * Cfg::kABytes, (uint32_t)(n * Cfg::kABytes), fb,
+                         pol_a);
+          } else if (n == G) {
             tma_tile_2d_g2s(smem_u32(a_dst), &tmAg, 0, y0, fb, pol_a);
             if (Cfg::kSplit) tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kAPart), &tmAlog, 0, y0, fb, pol_a);
           } else {
@@ -976,6 +982,7 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.parts = r.parts;
   p.counters = r.counters;
   p.scales = A.scales;
+  p.avals = static_cast<const uint8_t*>(A.vals);
   p.b_scale = e4 ? B.scale : 1.0f;
   p.K = A.K;
   if (r.items) {
