@@ -81,12 +81,9 @@ struct TcParams {
   const int* parts;
   unsigned* counters;
   // e4m3: A's per-block scales (powers of two; each block's UE8M0 scale factor
-  // is its exponent), B's scale (applied in the epilogue) and K (a partial
-  // group's spare panel slot is filled by a copy from row K, past the end of B,
-  // which reads zeros)
+  // is its exponent) and B's scale (applied in the epilogue)
   const float* scales;
   float b_scale;
-  int K;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* ptr) {
@@ -114,13 +111,16 @@ __device__ __forceinline__ void st_release_gpu(unsigned* ptr, unsigned v) {
 // whose second K half is zero on the A side (the block descriptor's
 // K-direction core-matrix stride points at a zeroed region after the group's
 // blocks) and, on the panel side, reads the next 2 KB of the slot: the next
-// 128-column slice, or a zero-filled panel slot / tail. A's per-block scale
-// (a power of two) becomes the MMA's B-side scale factor: a 512-byte tile of
-// its UE8M0 byte, written by B issuer 0 into the ring slot and moved to TMEM
-// with tcgen05.cp right before the block's MMAs. Every byte of the tile is the
-// same, so the factor does not depend on which TMEM cells the MMA reads. The
-// panel side's factor is a constant 1 (0x7F), copied once per CTA. B's scale
-// multiplies C in the epilogue.
+// 128-column slice, the next block's panel, or the slot's zero tail (a
+// partial group's panels fill the slot's last slots, so its last block is
+// followed by the tail too). A's per-block scale (a power of two) becomes the
+// MMA's B-side scale factor: a 512-byte tile whose every 32-bit word holds the
+// group's UE8M0 bytes (byte b for block b), written by one B issuer into the
+// ring slot and moved to TMEM with one tcgen05.cp per group; the MMA of block
+// b selects byte b with its scale-factor id. Every word is the same, so the
+// factor does not depend on which TMEM lanes the MMA reads. The panel side's
+// factor is a constant 1 (0x7F), copied once per CTA. B's scale multiplies C
+// in the epilogue.
 template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
 struct TcCfg {
   static constexpr bool kSplit = MODE == MODE_SPLIT;
@@ -134,27 +134,27 @@ struct TcCfg {
   static constexpr int kABytes = BR * (kE4 ? 16 : 32);   // bR rows x 16 elements
   static constexpr int kAPart = G * kABytes;          // one part (hi or lo) of a group's A blocks
   // fp16 / bf16 / split slot: [A (hi, lo) | B panels (hi, lo)]
-  // e4m3 slot: [A blocks | zeros (one block) | scale tiles | B panels | 2 KB zero tail]
+  // e4m3 slot: [A blocks | zeros (one block) | scale tile | B panels | 2 KB zero tail]
   static constexpr int kAZeroOff = kAPart;
   static constexpr int kScaleOff = kAZeroOff + kABytes;
-  static constexpr int kAStage = kE4 ? ((kScaleOff + G * 512 + 1023) / 1024) * 1024
+  static constexpr int kAStage = kE4 ? ((kScaleOff + 512 + 1023) / 1024) * 1024
                                      : ((kAPart * kParts + 1023) / 1024) * 1024;
   static constexpr int kTailOff = kAStage + G * kPanelBytes * kParts;
   static constexpr int kStage = kE4 ? ((kTailOff + 2048 + 1023) / 1024) * 1024 : kTailOff;
   // e4m3, after the ring: the panel-side scale tile (512 bytes of 0x7F)
   static constexpr int kExtra = kE4 ? 512 : 0;
   static constexpr int kAccCols = kJ * BR;            // TMEM columns of one accumulator
-  // e4m3 scale factors in TMEM: 4 columns for the panel side, 4 per block of the ring
+  // e4m3 scale factors in TMEM: 4 columns for the panel side, 4 per ring slot
   static constexpr int kSfaCol = ACC * kAccCols;
   static constexpr int kSfbCol = kSfaCol + 4;
-  static constexpr int kUsedCols = kE4 ? kSfbCol + 4 * STAGES * G : ACC * kAccCols;
+  static constexpr int kUsedCols = kE4 ? kSfbCol + 4 * STAGES : ACC * kAccCols;
   static constexpr int kTmemCols = kUsedCols <= 32 ? 32 : kUsedCols <= 64 ? 64 : kUsedCols <= 128 ? 128
                                    : kUsedCols <= 256 ? 256 : 512;
   static constexpr size_t kSmem = 1024 + (size_t)STAGES * kStage + kExtra + 1024;
   static_assert(kUsedCols <= 512, "TMEM columns");
   static_assert(NT % 128 == 0, "NT");
   static_assert(G * BR <= 256 && 32 % G == 0, "a group is one TMA box and never straddles an index chunk");
-  static_assert(!kE4 || G <= 4, "e4m3: a partial group's spare slot is copied by the B issuer of that slot");
+  static_assert(!kE4 || G <= 4, "e4m3: one scale byte per block in a 32-bit word");
   // kind::f16 instruction descriptor: D f32, A/B f16 or bf16, A MN-major, B K-major,
   // N = BR, M = 128.
   static constexpr uint32_t kIdescF16 = (1u << 4) | ((MODE == MODE_BF16 ? 1u : 0u) << 7) |
@@ -394,10 +394,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             break;
           }
           const uint32_t fb = full0 + 8 * s;
-          // e4m3: a partial group also fills panel slot n (zeros), which the
-          // last block's last slice reads as its K padding
-          const int panels = (Cfg::kE4 && n < G) ? n + 1 : n;
-          mbar_arrive_expect_tx(fb, (uint32_t)((n * Cfg::kABytes + panels * Cfg::kPanelBytes) * Cfg::kParts));
+          mbar_arrive_expect_tx(fb, (uint32_t)(n * (Cfg::kABytes + Cfg::kPanelBytes) * Cfg::kParts));
           uint8_t* a_dst = smem + (size_t)s * Cfg::kStage;
           const int y0 = j0 * BR;
           if constexpr (Cfg::kE4) {
@@ -483,9 +480,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
         for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
           const int n = min(G, cnt - i0);
-          // e4m3: a partial group also fills the next panel slot with zeros
-          // (the last block's last slice reads it as K padding)
-          const int nslots = (Cfg::kE4 && n < G) ? n + 1 : n;
           const int s = (int)(gs % STAGES);
           // Wait for the slot only in groups this issuer copies into: such a
           // group cannot be released without its bytes, so the slot's empty
@@ -493,7 +487,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           // groups it has no block in could fall two phases behind and miss a
           // parity flip.) Issuer 0 copies into every group, and so does the
           // e4m3 scale writer (its arrival is part of every group's full barrier).
-          const bool writes = bidx < nslots || (Cfg::kE4 && bidx == kScaleWriter);
+          const bool writes = bidx < n || (Cfg::kE4 && bidx == kScaleWriter);
           int bad = 0;
           if (lane == 0 && writes && gs >= (uint32_t)STAGES &&
               !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
@@ -503,8 +497,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           failed = __shfl_sync(0xffffffffu, bad, 0);
           if (failed) break;
           uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
-          for (int b = bidx; b < nslots; b += kBIssuers) {
-            const int col = __shfl_sync(0xffffffffu, cur, min(i0 + b, 31));
+          for (int b = bidx; b < n; b += kBIssuers) {
+            const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
             if constexpr (!Cfg::kSplit && !Cfg::kE4) {
               if (col < 0 && p.gather_rows) {
                 // Gather block: its panel is 16 arbitrary B rows. Lane L < 4 * (NT / 64)
@@ -529,10 +523,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             }
             if (lane == 0) {
               const uint32_t fb = full0 + 8 * s;
-              uint8_t* b_dst = b_dst0 + (size_t)b * Cfg::kPanelBytes * Cfg::kParts;
-              // the spare slot of a partial e4m3 group is copied from row K:
-              // every row of the box lies past the end of B and reads zeros
-              const int y = (Cfg::kE4 && b >= n) ? p.K : col * 16;
+              // e4m3: a partial group's panels take the slot's last slots
+              const int slot = Cfg::kE4 ? G - n + b : b;
+              uint8_t* b_dst = b_dst0 + (size_t)slot * Cfg::kPanelBytes * Cfg::kParts;
+              const int y = col * 16;
               if (p.panel3d) {
                 tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, y, nt * (NT / Cfg::kBoxCols), fb, pol_b);
                 if (Cfg::kSplit)
@@ -551,20 +545,21 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           }
           if constexpr (Cfg::kE4) {
             if (bidx == kScaleWriter) {
-              // After its own copies are in flight: one 512-byte tile per
-              // block, every byte the block scale's UE8M0 encoding, the
-              // exponent field of a power-of-two fp32 (bit 64 of the error
-              // word flags a scale that is not one); then the proxy fence that
-              // makes the tiles visible to tcgen05.cp, and the arrival the
+              // After its own copies are in flight: the group's 512-byte scale
+              // tile, every 32-bit word holding byte b = block b's scale in
+              // UE8M0, the exponent field of a power-of-two fp32 (bit 64 of
+              // the error word flags a scale that is not one); then the proxy
+              // fence that makes it visible to tcgen05.cp, and the arrival the
               // group's full barrier waits for.
-              uint8_t* tiles = smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff;
+              uint32_t w = 0;
               for (int b = 0; b < n; ++b) {
                 const uint32_t bits = __float_as_uint(__shfl_sync(0xffffffffu, cursc, i0 + b));
                 const uint32_t e = (bits >> 23) & 0xFFu;
                 if (lane == 0 && ((bits & 0x807FFFFFu) != 0u || e == 0u || e == 0xFFu)) atomicOr(p.err, 64u);
-                const uint32_t w = e * 0x01010101u;
-                *reinterpret_cast<uint4*>(tiles + b * 512 + 16 * lane) = make_uint4(w, w, w, w);
+                w |= e << (8 * b);
               }
+              *reinterpret_cast<uint4*>(smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff + 16 * lane) =
+                  make_uint4(w, w, w, w);
               fence_proxy_async_smem();
               __syncwarp();
               if (lane == 0) mbar_arrive(full0 + 8 * s);
@@ -602,26 +597,24 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           tc_fence_after();
           const uint32_t a_slot = smem_u32(smem + (size_t)s * Cfg::kStage);
           const uint32_t b_slot = a_slot + Cfg::kAStage;
-          if constexpr (Cfg::kE4) {
-            // the group's scale factors into their TMEM columns, ahead of its MMAs
-            for (int b = 0; b < n; ++b)
-              tmem_cp_32x128b_x4(tmem + Cfg::kSfbCol + (uint32_t)((s * G + b) * 4),
-                                 smem_desc(a_slot + Cfg::kScaleOff + b * 512, 128, 128, kLayoutNone));
-          }
+          // e4m3: the group's scale factors into the slot's TMEM columns, ahead of its MMAs
+          const uint32_t sfb = tmem + Cfg::kSfbCol + (uint32_t)(s * 4);
+          if constexpr (Cfg::kE4)
+            tmem_cp_32x128b_x4(sfb, smem_desc(a_slot + Cfg::kScaleOff, 128, 128, kLayoutNone));
           for (int b = 0; b < n; ++b) {
-            const uint32_t b_addr = b_slot + b * Cfg::kPanelBytes * Cfg::kParts;
+            const uint32_t b_addr = b_slot + (Cfg::kE4 ? G - n + b : b) * Cfg::kPanelBytes * Cfg::kParts;
             const uint32_t accum = (j0 + b != start) ? 1u : 0u;
             if constexpr (Cfg::kE4) {
               // one K = 32 MMA per slice: K 0..15 the block (K-major, no
               // swizzle, 8-row core matrices 128 bytes apart), K 16..31 the
-              // slot's zero block; the block's scale factor from its columns
-              const uint32_t sfb = tmem + Cfg::kSfbCol + (uint32_t)((s * G + b) * 4);
+              // slot's zero block; scale-factor id b picks the block's byte
               const uint32_t blk = a_slot + b * Cfg::kABytes;
               const uint64_t blk_d = smem_desc(blk, a_slot + Cfg::kAZeroOff - blk, 128, kLayoutNone);
 #pragma unroll
               for (int j = 0; j < Cfg::kJ; ++j) {
                 const uint64_t pan = smem_desc(b_addr + j * Cfg::kSliceBytes, 1024, 1024, kLayoutSW128);
-                umma_mxf8_scaled(d0 + j * BR, pan, blk_d, Cfg::kIdesc, tmem + Cfg::kSfaCol, sfb, accum);
+                umma_mxf8_scaled(d0 + j * BR, pan, blk_d, Cfg::kIdesc | ((uint32_t)b << 4), tmem + Cfg::kSfaCol,
+                                 sfb, accum);
               }
               continue;
             }
@@ -984,7 +977,6 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.scales = A.scales;
   p.avals = static_cast<const uint8_t*>(A.vals);
   p.b_scale = e4 ? B.scale : 1.0f;
-  p.K = A.K;
   if (r.items) {
     if (p.split > 1 || r.csr || r.gather_rows || (p.queue && !r.queue))
       return fail(SPMM_ERR_UNSUPPORTED, "a planned product runs without split-K, CSR part or shared work queue");
