@@ -51,7 +51,10 @@ typedef struct spmm_config {
   int stages;    /* pipeline depth 2..8 (0 = auto)                                   */
   int ctas_per_sm; /* persistent grid = SMs x this (0 = auto)                          */
   int acc_buffers; /* tcgen05: TMEM accumulators per CTA, 1 or 2 (0 = auto)          */
-  int schedule;    /* tcgen05: 0 = static item stride, 1 = atomic work queue         */
+  int schedule;    /* tcgen05: 0 = static item stride, 1 = atomic work queue,
+                      2 = per-matrix plan (a tuner-table mark: spmm_bcsr_plan_create
+                      builds the plan, whose runs chain with
+                      SPMM_RUN_INPUTS_READY; spmm_bcsr_mm runs it as 1)       */
   int split_k;     /* tcgen05: split each block row's blocks over this many work
                       items whose partial products are added into C (C is
                       zeroed first; the order of the additions varies from run
@@ -315,11 +318,25 @@ spmm_status spmm_config_supported(int bR, spmm_dtype dtype, int N, const spmm_co
 /* Exhaustive sweep: times every table entry on this product. Per entry:
  * `warmup` untimed runs, then `reps` runs each preceded (when flush != NULL)
  * by a write of flush_bytes to `flush` (evicting L2) and timed alone with CUDA
- * events; ms_out[i] = the mean, +inf where the entry has no kernel.
+ * events; ms_out[i] = the mean, +inf where the entry has no kernel. A plan
+ * entry (schedule 2) builds the plan once and times its runs.
  * Overwrites C; synchronises the stream. */
 spmm_status spmm_tune_sweep(const spmm_bcsr_desc* A, const spmm_dense_desc* B, int N, float* C, int ldc,
                             int warmup, int reps, void* flush, size_t flush_bytes, float* ms_out,
                             void* stream);
+
+/* Back-to-back sweep: times every table entry as `launches` consecutive
+ * products over the `ncopies` copies of one problem (copy k % ncopies for
+ * launch k; copies large enough together to exceed L2 make every launch read
+ * its inputs from HBM), captured in one CUDA graph and replayed after `warmup`
+ * eager runs and one untimed replay (launches issued one by one if capture
+ * fails). Plan entries (schedule 2) build one plan from copies[0] and chain
+ * their runs with SPMM_RUN_INPUTS_READY. ms_out[i] = the mean time per launch,
+ * +inf where the entry has no kernel. This is the regime of a caller that
+ * runs product after product on one stream. Overwrites every copy's C;
+ * synchronises. */
+spmm_status spmm_tune_sweep_b2b(const spmm_problem* copies, int ncopies, int launches, int warmup,
+                                float* ms_out, void* stream);
 
 /* Structure features (18 floats) of the product A (M x K, bR x 16 blocks,
  * element type dtype) x B (K x N), the cost model's input. The _host variant

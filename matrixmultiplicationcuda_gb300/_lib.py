@@ -128,6 +128,7 @@ _SIGS = {
     "spmm_config_supported": (c_int, [c_int, c_int, c_int, ctypes.POINTER(Config)]),
     "spmm_tune_sweep": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp, c_int, c_int,
                                 c_int, c_vp, c_size, c_vp, c_vp]),
+    "spmm_tune_sweep_b2b": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_vp]),
     "spmm_structure_features": (c_int, [ctypes.POINTER(BcsrDesc), c_int, c_vp, c_vp]),
     "spmm_mlp_param_count": (c_ll, [ctypes.POINTER(MlpShape)]),
     "spmm_mlp_workspace_floats": (c_ll, [ctypes.POINTER(MlpShape), c_int]),

@@ -197,7 +197,7 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   std::memset(&c, 0, sizeof(c));
   if (cfg) c = *cfg;
   if (c.kernel != 0 && c.kernel != 2) return fail(SPMM_ERR_UNSUPPORTED, "a plan runs on kernel 2");
-  if (c.split_k > 1 || (c.schedule != 0 && c.schedule != 1))
+  if (c.split_k > 1 || c.schedule < 0 || c.schedule > 2)
     return fail(SPMM_ERR_UNSUPPORTED, "a plan replaces split-K and brings its own work queue");
   c.kernel = 2;
   c.schedule = 1;   // the plan's queue

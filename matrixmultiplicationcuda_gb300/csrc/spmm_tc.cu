@@ -826,7 +826,8 @@ const TcEntry kTcEntries[] = {
     SPMM_TC_ENTRY(64, 256, 7, MODE_E4M3, 1, 2), SPMM_TC_ENTRY(64, 512, 9, MODE_E4M3, 1, 2),
     SPMM_TC_ENTRY(64, 256, 8, MODE_E4M3, 2, 2), SPMM_TC_ENTRY(64, 128, 8, MODE_E4M3, 2, 2),
     SPMM_TC_ENTRY(64, 256, 4, MODE_E4M3, 1, 4), SPMM_TC_ENTRY(64, 512, 4, MODE_E4M3, 1, 4),
-    SPMM_TC_ENTRY(32, 256, 3, MODE_E4M3, 1, 4), SPMM_TC_ENTRY(16, 256, 3, MODE_E4M3, 2, 4),
+    SPMM_TC_ENTRY(32, 256, 4, MODE_E4M3, 1, 4), SPMM_TC_ENTRY(16, 256, 4, MODE_E4M3, 1, 4),
+    SPMM_TC_ENTRY(16, 256, 3, MODE_E4M3, 2, 4),
 };
 
 int tc_mode(spmm_dtype d) {
@@ -961,7 +962,7 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.err = r.err_word ? r.err_word : device_error_word();
   p.panel3d = panel3d;
   // items: static stride by default, or a work queue on request
-  p.queue = r.queue ? r.queue : (r.cfg.schedule == 1 ? work_queue_slot() : nullptr);
+  p.queue = r.queue ? r.queue : (r.cfg.schedule >= 1 ? work_queue_slot() : nullptr);
   p.claim_ahead = e->stages - 1;
   p.inputs_ready = r.inputs_ready ? 1 : 0;
   p.csr_row_ptr = r.csr ? r.csr->row_ptr : nullptr;

@@ -42,8 +42,15 @@ def config_name(c):
         return "mma nt%d st%d" % (c.n_tile, c.stages)
     if c.kernel == 3:
         return "tc64 nt%d %s" % (c.n_tile, "queue" if c.schedule else "static")
+    if c.schedule == 2:
+        return "plan tc nt%d st%s acc%d" % (c.n_tile, c.stages or "d", c.acc_buffers)
     return "tc nt%d st%s acc%d %s split%d" % (c.n_tile, c.stages or "d", c.acc_buffers,
                                              "queue" if c.schedule else "static", max(c.split_k, 1))
+
+
+def is_plan(c):
+    """A table entry that runs as a per-matrix plan (schedule 2)."""
+    return c.kernel == 2 and c.schedule == 2
 
 
 def supported_mask(bR, dtype, N):
@@ -99,6 +106,30 @@ def sweep(A, B, N=None, C=None, warmup=2, reps=5, flush=None, stream=None, B_lo=
     check(lib().spmm_tune_sweep(ctypes.byref(a), ctypes.byref(b), N, ctypes.c_void_p(C.data_ptr()),
                                 int(C.stride(0)), warmup, reps, fptr, fbytes,
                                 ctypes.c_void_p(ms.ctypes.data), stream_handle(stream)))
+    return ms
+
+
+def sweep_b2b(copies, launches=20, warmup=2, stream=None):
+    """Mean time per launch (ms) of every table entry run back to back over
+    `copies` -- a list of (A, B, C) or (A, B, C, B_lo, b_scale) of one problem
+    -- replayed from a CUDA graph (spmm_tune_sweep_b2b); +inf where
+    unsupported. Plan entries (schedule 2) chain their runs with the
+    inputs-ready flag."""
+    from ._lib import Problem
+    from .bcsr import _dense_desc
+    arr = (Problem * len(copies))()
+    for i, cp in enumerate(copies):
+        A, B, C = cp[:3]
+        B_lo = cp[3] if len(cp) > 3 else None
+        bs = cp[4] if len(cp) > 4 else 1.0
+        arr[i].A = A.desc()
+        arr[i].B = _dense_desc(B, B_lo, bs, ldb=B.stride(0))
+        arr[i].N = int(B.shape[1])
+        arr[i].C = C.data_ptr()
+        arr[i].ldc = int(C.stride(0))
+    ms = np.zeros(n_configs(), np.float32)
+    check(lib().spmm_tune_sweep_b2b(arr, len(copies), int(launches), int(warmup), ctypes.c_void_p(ms.ctypes.data),
+                                    stream_handle(stream)))
     return ms
 
 

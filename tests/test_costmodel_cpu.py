@@ -80,7 +80,8 @@ def test_features_reject_bad_structure():
 
 def test_config_table():
     cs = tuner.configs()
-    assert len(cs) == 41
+    assert len(cs) == 56
+    assert sum(tuner.is_plan(c) for c in cs) == 7
     keys = {tuner.config_key(c) for c in cs}
     assert len(keys) == len(cs)
     for bR in (16, 32, 64):
@@ -88,7 +89,8 @@ def test_config_table():
             mask = tuner.supported_mask(bR, dt, 512)
             assert mask.any()
             assert mask[tuner.default_index(bR, dt, 512)]
-    assert tuner.supported_mask(64, m.DType.F16, 512).sum() == 40
+    assert tuner.supported_mask(64, m.DType.F16, 512).sum() == 45
+    assert tuner.supported_mask(64, m.DType.E4M3, 512).sum() == 35
 
 
 def test_tune_db_roundtrip(tmp_path):

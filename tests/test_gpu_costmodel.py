@@ -127,6 +127,40 @@ def test_sweep_times_supported_configs(dev, bR):
     assert mx <= 1e-5 and fr <= 1e-5
 
 
+@pytest.mark.parametrize("bR,dtype", [(64, m.DType.F16), (16, m.DType.F16), (64, m.DType.E4M3)])
+def test_back_to_back_sweep(dev, bR, dtype):
+    """spmm_tune_sweep_b2b: every supported entry (plans included) timed over
+    rotating copies, +inf elsewhere, and every copy's C left correct."""
+    M, K, N = 1024, 2048, 256
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_RANDOM, 0.05, 0, seed=13)
+    vals = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=14)
+    Bf = m.gen_dense(K, N, m.DIST_UNIFORM, seed=15)
+    copies = []
+    for _ in range(3):
+        A = m.BCSR.from_host(M, K, bR, rp, ci, vals, dtype, device=dev)
+        Bq, _, Bs = m.quantize(torch.from_numpy(Bf).to(dev).reshape(-1), dtype)
+        copies.append((A, Bq.view(K, N), torch.full((M, N), float("nan"), device=dev), None,
+                       float(Bs[0]) if Bs is not None else 1.0))
+    ms = tuner.sweep_b2b(copies, launches=6, warmup=1)
+    m.device_error_check()
+    mask = tuner.supported_mask(bR, dtype, N)
+    assert np.all(np.isfinite(ms[mask])) and np.all(ms[mask] > 0)
+    assert np.all(np.isinf(ms[~mask]))
+    assert any(tuner.is_plan(c) for c, ok in zip(tuner.configs(), mask) if ok)
+    A0 = copies[0][0]
+    if dtype == m.DType.E4M3:
+        sv = A0.vals.view(torch.float8_e4m3fn).double().cpu().numpy().reshape(-1, bR * 16)
+        sv = (sv * A0.scales.double().cpu().numpy()[:, None]).reshape(-1)
+        sB = copies[0][1].view(torch.float8_e4m3fn).double().cpu().numpy() * copies[0][4]
+    else:
+        sv = A0.vals.double().cpu().numpy()
+        sB = copies[0][1].double().cpu().numpy()
+    ref = oracle.bcsr_matmul_f64(rp, ci, sv, bR, 16, sB)
+    for A, B, C, _, _ in copies:
+        mx, fr = oracle.rel_errors(C.cpu().numpy(), ref)
+        assert mx <= 1e-5 and fr <= 1e-5
+
+
 def test_cost_model_select_returns_supported_config(dev):
     s, p, _, _, _, _ = _random_model(7)
     cm = costmodel.CostModel(s, p)
