@@ -250,7 +250,7 @@ def collect(specs, warmup=2, reps=5, device="cuda", progress=None, gpu_structure
         else:
             rp, ci = gen_structure(s["M"], s["K"], s["bR"], s["pattern"], s["density"], s["param"], seed=s["seed"])
             rpd, cid = torch.as_tensor(rp).to(device), torch.as_tensor(ci).to(device)
-        nvals = max(len(ci) * s["bR"] * 16, 1)
+        nvals = max(len(ci) * s["bR"] * 16, 256)     # each copy's slice starts 16-byte aligned
         KN, MN = s["K"] * s["N"], s["M"] * s["N"]
         esz = 1 if dt == DType.E4M3 else 2
         nbytes = nvals * esz * (2 if dt == DType.F16_SPLIT else 1) + KN * esz + MN * 4

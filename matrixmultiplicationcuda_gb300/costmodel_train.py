@@ -2,10 +2,12 @@
 
     python -m matrixmultiplicationcuda_gb300.costmodel_train [--out DIR]
         [--n-train 2000] [--n-test 500] [--seed 11] [--steps 8000]
-        [--dataset PATH]   # reuse collected sweeps instead of collecting
+        [--mode b2b|cold] [--dataset PATH]   # reuse collected sweeps instead of collecting
 
 1. Draws n_train + n_test seeded synthetic products (costmodel.sample_specs)
-   and sweeps every tuner configuration on each (the autotuner's own timings).
+   and sweeps every tuner configuration on each (the autotuner's own timings),
+   by default back to back over rotating copies with plans chained by the
+   inputs-ready flag (the regime of the benchmark's timed loop).
 2. Trains the MLP on the first n_train with the library's CUDA kernels.
 3. On the n_test held-out products compares three ways of choosing a
    configuration against the exhaustive sweep's best: the trained model, the
@@ -75,6 +77,7 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--steps", type=int, default=8000)
     ap.add_argument("--dataset", default=None)
+    ap.add_argument("--mode", default="b2b", choices=["b2b", "cold"])
     args = ap.parse_args(argv)
     import torch
     os.makedirs(args.out, exist_ok=True)
@@ -88,15 +91,16 @@ def main(argv=None):
     else:
         str_ = costmodel.sample_specs(args.n_train, args.seed)
         ste = costmodel.sample_specs(args.n_test, args.seed + 1)
-        Ftr, Ttr, ntr = costmodel.collect(str_, progress=250)
-        Fte, Tte, nte = costmodel.collect(ste, progress=250)
+        Ftr, Ttr, ntr = costmodel.collect(str_, progress=250, mode=args.mode)
+        Fte, Tte, nte = costmodel.collect(ste, progress=250, mode=args.mode)
         arrays = {}
         for pfx, sp in (("tr_", str_), ("te_", ste)):
             for k, v in spec_arrays(sp).items():
                 arrays[pfx + k] = v
         np.savez_compressed(os.path.join(args.out, "tune_dataset.npz"), F_train=Ftr, T_train=Ttr,
                             nnzb_train=ntr, F_test=Fte, T_test=Tte, nnzb_test=nte,
-                            device=np.array(torch.cuda.get_device_name()), **arrays)
+                            device=np.array(torch.cuda.get_device_name()), regime=np.array(args.mode),
+                            **arrays)
     t_collect = time.time() - t0
 
     s = costmodel.shape()
@@ -127,6 +131,7 @@ def main(argv=None):
     fixed_pick = np.where(Mte[:, fixed] > 0, fixed, heur)
     report = {
         "device": torch.cuda.get_device_name(),
+        "regime": (str(z["regime"]) if args.dataset and "regime" in z.files else args.mode),
         "n_train": len(Ftr), "n_test": len(Fte), "configs": tuner.n_configs(),
         "features": tuner.N_FEATURES, "hidden": s.hidden, "layers": s.layers, "steps": args.steps,
         "collect_s": t_collect, "train_s": t_train,
