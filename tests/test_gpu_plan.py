@@ -91,10 +91,14 @@ def test_plan_rejects(dev):
     rp, ci = m.gen_structure(M, K, 64, m.PATTERN_RANDOM, 0.1, 0, seed=1)
     vals = m.gen_values(len(ci), 64, 16, m.DIST_UNIFORM, seed=2)
     A = m.BCSR.from_host(M, K, 64, rp, ci, vals, m.DType.F16, device=dev)
-    for cfg in (m.Config(kernel=1), m.Config(kernel=2, split_k=2), m.Config(kernel=2, schedule=2)):
+    for cfg in (m.Config(kernel=1), m.Config(kernel=2, split_k=2), m.Config(kernel=2, schedule=3)):
         with pytest.raises(m.SpmmError) as e:
             m.BcsrPlan(A, 256, cfg)
         assert e.value.status == m.Status.UNSUPPORTED
+    # schedule 2 (the tuner table's mark for a plan entry) builds the plan too
+    p2 = m.BcsrPlan(A, 256, m.Config(kernel=2, schedule=2))
+    assert p2.info()[2].schedule == 1
+    p2.close()
     plan = m.BcsrPlan(A, 256)
     assert plan.info()[2].schedule == 1                    # the plan's own work queue
     m.BcsrPlan(A, 256, plan.info()[2]).close()             # what it reports builds another plan
