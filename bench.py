@@ -578,18 +578,22 @@ def run_ours(args, world, rank, local):
 
     # End to end through the public API with host buffers (pinned), tuned precision:
     # every step copies its inputs host -> device, multiplies, and reads C back.
-    # Two streams with their own device buffers alternate, so one step's copies
-    # overlap the other's kernel (the copy engines run both directions at once).
+    # Three device buffer sets rotate through three streams -- uploads, products,
+    # downloads -- ordered by events, so the host link carries one step's inputs
+    # in while an earlier step's C comes out (the copy engines run both
+    # directions at once) and no stream's next upload waits behind its own
+    # download.
     A0, Bq0, Blo0, bs0, C0 = probs[0]
     hA = [t.cpu().pin_memory() for t in (A0.row_ptr, A0.col_idx, A0.vals)]
     hx = [t.cpu().pin_memory() for t in (A0.vals_lo, A0.scales) if t is not None]
     hB = [t.cpu().pin_memory() for t in (Bq0, Blo0) if t is not None]
-    hC = [torch.empty((M, N), dtype=torch.float32).pin_memory() for _ in range(2)]
+    nsets = 3
+    hC = [torch.empty((M, N), dtype=torch.float32).pin_memory() for _ in range(nsets)]
     h2d = sum(t.numel() * t.element_size() for t in hA + hx + hB)
     d2h = hC[0].numel() * 4
-    streams = [torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)]
+    up, comp, down = (torch.cuda.Stream(device=dev) for _ in range(3))
     sets = []
-    for k in range(2):
+    for k in range(nsets):
         dA = [torch.empty_like(t, device=dev) for t in hA]
         dx = [torch.empty_like(t, device=dev) for t in hx]
         dB = [torch.empty_like(t, device=dev) for t in hB]
@@ -597,21 +601,28 @@ def run_ours(args, world, rank, local):
                     dx[0] if A0.vals_lo is not None else None,
                     dx[-1] if A0.scales is not None else None)
         sets.append((dA + dx + dB, Ae, dB, torch.empty((M, N), dtype=torch.float32, device=dev)))
-
-    # a plan runs one launch at a time (its work queue is its own): one per stream
-    e2e_cfgs = [cfg, cfg]
-    if isinstance(cfg, m.BcsrPlan):
-        e2e_cfgs[1] = m.BcsrPlan(A0, N, cfg.info()[2])
+    ev_in = [torch.cuda.Event() for _ in range(nsets)]     # set k's inputs are on the device
+    ev_done = [torch.cuda.Event() for _ in range(nsets)]   # set k's product is in its C
+    ev_free = [torch.cuda.Event() for _ in range(nsets)]   # set k's C has reached the host
+    used = [False] * nsets
 
     def e2e_step(i):
-        dev_bufs, Ae, dB, Cd = sets[i % 2]
-        st = streams[i % 2]
-        with torch.cuda.stream(st):
+        k = i % nsets
+        dev_bufs, Ae, dB, Cd = sets[k]
+        if used[k]:
+            up.wait_event(ev_free[k])       # the set's last C has left before it is refilled
+        with torch.cuda.stream(up):
             for d, h in zip(dev_bufs, hA + hx + hB):
                 d.copy_(h, non_blocking=True)
-            launch((Ae, dB[0], dB[1] if len(dB) > 1 else None, bs0, Cd), e2e_cfgs[i % 2], stream=st,
-                   inputs_ready=False)
-            hC[i % 2].copy_(Cd, non_blocking=True)
+            ev_in[k].record(up)
+        comp.wait_event(ev_in[k])
+        launch((Ae, dB[0], dB[1] if len(dB) > 1 else None, bs0, Cd), cfg, stream=comp, inputs_ready=False)
+        ev_done[k].record(comp)
+        down.wait_event(ev_done[k])
+        with torch.cuda.stream(down):
+            hC[k].copy_(Cd, non_blocking=True)
+            ev_free[k].record(down)
+        used[k] = True
 
     e2e_steps = max(4, min(args.steps, 50))
     for i in range(4):
@@ -620,11 +631,11 @@ def run_ours(args, world, rank, local):
     barrier(world)
     q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     q0.record(stream)
-    for st in streams:
+    for st in (up, comp, down):
         st.wait_event(q0)
     for i in range(e2e_steps):
         e2e_step(i)
-    for st in streams:
+    for st in (up, comp, down):
         ev = torch.cuda.Event()
         ev.record(st)
         stream.wait_event(ev)
