@@ -40,9 +40,10 @@
 //       cuBLAS GemmEx.
 //   hybrid  the hybrid BCSR + CSR product across density thresholds.
 //
-// Tunings: default (the library's choice), model (the cost model's pick),
-// plan (a per-matrix plan on each tcgen05 configuration of the tuner's table
-// without split-K, the fastest reported), sweep (the exhaustive sweep's best).
+// Tunings: default (the library's choice), model (the cost model's pick from
+// the tuner table; a plan entry is built once and its runs are timed), plan
+// (each per-matrix plan entry of the tuner table, the fastest reported),
+// sweep (the exhaustive cold sweep's best).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
@@ -151,6 +152,8 @@ std::string config_name(const spmm_config* c) {
     std::snprintf(b, sizeof(b), "mma nt%d st%d", c->n_tile, c->stages);
   else if (c->kernel == 3)
     std::snprintf(b, sizeof(b), "tc64 nt%d %s", c->n_tile, c->schedule ? "queue" : "static");
+  else if (c->schedule == 2)
+    std::snprintf(b, sizeof(b), "plan tc nt%d st%d acc%d", c->n_tile, c->stages, c->acc_buffers);
   else
     std::snprintf(b, sizeof(b), "tc nt%d st%d acc%d %s split%d", c->n_tile, c->stages, c->acc_buffers,
                   c->schedule ? "queue" : "static", c->split_k > 1 ? c->split_k : 1);
@@ -460,7 +463,7 @@ class Runner {
         for (int i = 0; i < spmm_tune_config_count(); ++i) {
           spmm_config tc{};
           SK(spmm_tune_config(i, &tc));
-          if (tc.kernel != 2 || tc.split_k > 1 || tc.schedule != 0) continue;
+          if (tc.kernel != 2 || tc.schedule != 2) continue;   // the table's plan entries
           spmm_bcsr_plan* plan = nullptr;
           if (spmm_bcsr_plan_create(&P.A, P.N, &tc, nullptr, &plan) != SPMM_OK) continue;   // no kernel for it
           const Sample smp = timer_.measure([&] { SK(spmm_bcsr_plan_run(plan, &P.A, &P.B, P.N, P.C, P.N, nullptr)); }, o_);
@@ -479,6 +482,14 @@ class Runner {
         r.config = "plan " + config_name(&pcfg) + " (" + std::to_string(groups) + " rows split)";
         SK(spmm_bcsr_plan_run(best, &P.A, &P.B, P.N, P.C, P.N, nullptr));
         SK(spmm_bcsr_plan_destroy(best));
+      } else if (pc && pc->kernel == 2 && pc->schedule == 2) {
+        // a plan entry (the cost model's or the sweep's pick): build its plan
+        // once, time its runs
+        spmm_bcsr_plan* plan = nullptr;
+        SK(spmm_bcsr_plan_create(&P.A, P.N, pc, nullptr, &plan));
+        r.config = config_name(pc);
+        r.s = timer_.measure([&] { SK(spmm_bcsr_plan_run(plan, &P.A, &P.B, P.N, P.C, P.N, nullptr)); }, o_);
+        SK(spmm_bcsr_plan_destroy(plan));
       } else {
         r.config = config_name(pc);
         r.s = timer_.measure([&] { SK(spmm_bcsr_mm(&P.A, &P.B, P.N, P.C, P.N, pc, nullptr)); }, o_);
