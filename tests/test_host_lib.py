@@ -207,6 +207,18 @@ def test_nvbench_benches_registered():
     assert "PAT=[0,1,2,3,4,5,6]" in r.stdout and "SPARS=[60,70,80,90]" in r.stdout
 
 
+def test_nvbench_benches_argument_errors():
+    """The NVBench layer rejects an unknown bench, an unknown axis and a bad
+    axis value before touching the GPU (exit status 2)."""
+    exe = os.path.join(os.path.dirname(m.lib_path), "spmm_nvbench_benches")
+    for args in (["-b", "noSuchBench"], ["-b", "sparseMatrixMulTensor", "-a", "Q=[1]"],
+                 ["-b", "sparseMatrixMulTensor", "-a", "M"], ["--no-such-option"]):
+        r = subprocess.run([exe] + args, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2, (args, r.stdout, r.stderr)
+    r = subprocess.run([exe, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "--axis" in r.stdout
+
+
 def test_harness_built_and_prints_usage():
     exe = os.path.join(os.path.dirname(m.lib_path), "spmm_nvbench")
     assert os.path.exists(exe)
