@@ -140,6 +140,10 @@ __device__ __forceinline__ void tma_tile_3d_g2s(uint32_t dst, const void* tmap, 
       "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(bar), "l"(policy)
       : "memory");
 }
+// Prefetch [src, src + bytes) into L2 (bulk; 16-byte aligned start, bytes % 16 == 0).
+__device__ __forceinline__ void tma_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void tma_prefetch_desc(const void* tmap) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
 }
