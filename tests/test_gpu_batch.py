@@ -63,7 +63,7 @@ def check_fp64(probs, host, name, bar=3e-5):
 
 
 @pytest.mark.parametrize("name", ["f16", "bf16"])
-@pytest.mark.parametrize("stages,n_tile", [(0, 0), (2, 0), (8, 0), (0, 128), (0, 256)])
+@pytest.mark.parametrize("stages,n_tile", [(0, 0), (4, 0), (8, 0), (0, 128), (0, 256)])
 def test_batch_matches_fp64(dev, name, stages, n_tile):
     probs, host = build_small(dev, name)
     plan = m.BatchPlan(probs, cfg=m.Config(stages=stages, n_tile=n_tile))
