@@ -18,13 +18,15 @@
 //     in the K-major canonical layout (8-row groups 256 B apart); the blocks
 //     of a group are contiguous in memory and arrive in one copy.
 //
-// Warp roles (10 warps, two CTAs per SM): warp 0 takes items (static stride,
+// Warp roles (11 warps, two CTAs per SM): warp 0 takes items (static stride,
 // or from a work queue a few groups before the current item is copied),
 // publishes them through an item ring and copies A groups;
 // warps 2, 3, 8, 9 copy the B panels (a TMA instruction holds its issuing
 // thread for ~200 ns, so four threads share them); warp 1 (one thread) issues
-// the UMMAs, releases each group's ring slot with tcgen05.commit and hands
-// finished accumulators to the epilogue; warp 2 owns the TMEM allocation;
+// the UMMAs -- with warp 10 taking half of each block's 128-column slices when
+// there are two or more and no per-group scale copy -- releases each group's
+// ring slot with tcgen05.commit and hands finished accumulators to the
+// epilogue; warp 2 owns the TMEM allocation;
 // warps 4-7 drain TMEM (double-buffered, so the next item's MMAs overlap) with
 // tcgen05.ld and store C with streaming stores. Items = (block row, NT-column
 // tile). Every mbarrier wait is bounded; a wait that gives up sets the device
@@ -127,6 +129,14 @@ struct TcCfg {
   static constexpr bool kE4 = MODE == MODE_E4M3;
   static constexpr int kParts = kSplit ? 2 : 1;
   static constexpr int kJ = NT / 128;                 // 128-column MMA slices per item
+  // UMMA issuing threads: one thread's issue rate bounds the pipeline (a UMMA
+  // takes the issuing thread ~74 cycles; doubling each block's UMMAs slowed
+  // the headline plan by 17 %, while the same count at a quarter of the tensor
+  // work saved 1-2 %), so two warps split each block's slices: disjoint
+  // accumulators, the same sums. e4m3 keeps one: its per-group scale-factor
+  // copy must precede the group's MMAs in one thread's issue order.
+  static constexpr int kIssuers = (kE4 || kJ < 2) ? 1 : 2;
+  static constexpr int kJPer = kJ / kIssuers;         // slices per issuer
   static constexpr int kBoxBytes = 16 * 128;          // 16 rows x 128 bytes: 64 fp16 or 128 e4m3 columns
   static constexpr int kBoxCols = kE4 ? 128 : 64;
   static constexpr int kPanelBytes = (NT / kBoxCols) * kBoxBytes;
@@ -167,7 +177,7 @@ struct TcCfg {
   static constexpr uint32_t kIdesc = kE4 ? kIdescE4 : kIdescF16;
 };
 
-constexpr int kTcThreads = 320;   // 10 warps
+constexpr int kTcThreads = 352;   // 11 warps
 
 template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
 __global__ void __launch_bounds__(kTcThreads, 2)
@@ -198,16 +208,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       // the lead's arrive (it expects the whole group's bytes); e4m3 also B
       // issuer 0's, after it has written the group's scale tiles
       mbar_init(full0 + 8 * s, Cfg::kE4 ? 2 : 1);
-      mbar_init(empty0 + 8 * s, 1);           // the MMA thread's commit
+      mbar_init(empty0 + 8 * s, Cfg::kIssuers);   // each MMA issuer's commit
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tfull0 + 8 * b, Cfg::kIssuers);
       mbar_init(tempty0 + 8 * b, 4);
     }
-    mbar_init(done_bar, 1);
+    mbar_init(done_bar, Cfg::kIssuers);
     for (int q = 0; q < kQ; ++q) {
       mbar_init(qfull0 + 8 * q, 1);
-      mbar_init(qempty0 + 8 * q, 1 + kBIssuers + 4);   // MMA, B issuers, epilogue warps
+      mbar_init(qempty0 + 8 * q, Cfg::kIssuers + kBIssuers + 4);   // MMA issuers, B issuers, epilogue warps
     }
     fence_mbar_init();
   }
@@ -251,12 +261,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   // launch). With inputs_ready the caller promises that no kernel launched on
   // the stream since its last host synchronisation writes A or B, so the
   // warps that read only A and B or work in
-  // shared memory and TMEM (lead, MMA, B issuers) start at once: a CTA copies
+  // shared memory and TMEM (lead, both MMA issuers, B issuers) start at once: a CTA copies
   // and multiplies its first item while the previous kernel finishes. The lead
   // waits before its first work-queue claim and the epilogue before it touches
   // C or a split row's counters, so the queue, the counters and C keep their
   // order with the previous kernel.
-  const bool early = p.inputs_ready && (warp <= 3 || warp == 8 || warp == 9);
+  const bool early = p.inputs_ready && (warp <= 3 || warp >= 8);
   if (!early) grid_dep_wait();
   bool dep_waited = !early;
 
@@ -575,9 +585,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
       }
     }
-  } else if (warp == 1) {
-    // ------------------------------ MMA issuer -----------------------------------
+  } else if (warp == 1 || (Cfg::kIssuers == 2 && warp == 10)) {
+    // ------------------------------ MMA issuers ----------------------------------
+    // Issuer i takes 128-column slices [i * kJPer, (i + 1) * kJPer) of every
+    // block; each commits its own MMAs to the slot, accumulator and done
+    // barriers, which expect one commit per issuer.
     if (lane == 0) {
+      const int jb = warp == 1 ? 0 : Cfg::kJPer;
       uint32_t gs = 0, it = 0;
       bool failed = false;
       if constexpr (Cfg::kE4)   // the panel side's scale factors: 1.0 for every row
@@ -618,7 +632,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
               const uint32_t blk = a_slot + b * Cfg::kABytes;
               const uint64_t blk_d = smem_desc(blk, a_slot + Cfg::kAZeroOff - blk, 128, kLayoutNone);
 #pragma unroll
-              for (int j = 0; j < Cfg::kJ; ++j) {
+              for (int jj = 0; jj < Cfg::kJPer; ++jj) {
+                const int j = jb + jj;
                 const uint64_t pan = smem_desc(b_addr + j * Cfg::kSliceBytes, 1024, 1024, kLayoutSW128);
                 umma_mxf8_scaled(d0 + j * BR, pan, blk_d, Cfg::kIdesc | ((uint32_t)b << 4), tmem + Cfg::kSfaCol,
                                  sfb, accum);
@@ -627,7 +642,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             }
             const uint64_t blk_hi = smem_desc(a_slot + b * Cfg::kABytes, 16, 256, kLayoutSW32);
 #pragma unroll
-            for (int j = 0; j < Cfg::kJ; ++j) {
+            for (int jj = 0; jj < Cfg::kJPer; ++jj) {
+              const int j = jb + jj;
               const uint64_t pan_hi = smem_desc(b_addr + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
               umma_f16(d0 + j * BR, pan_hi, blk_hi, Cfg::kIdesc, accum);
               if constexpr (Cfg::kSplit) {
@@ -645,7 +661,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         if (failed) break;
         umma_commit(tfull0 + 8 * acc);   // accumulator ready (immediately, for an empty row)
       }
-      // every MMA this thread issued has completed before TMEM is released
+      // every MMA the issuers issued has completed before TMEM is released
       umma_commit(done_bar);
       if (!mbar_wait(done_bar, 0, p.timeout_ns)) atomicOr(p.err, 8u);
     }
