@@ -24,7 +24,7 @@
 // warps 2, 3, 8, 9 copy the B panels (a TMA instruction holds its issuing
 // thread for ~200 ns, so four threads share them); warp 1 (one thread) issues
 // the UMMAs -- with warp 10 taking half of each block's 128-column slices when
-// there are two or more and no per-group scale copy -- releases each group's
+// there are two or more -- releases each group's
 // ring slot with tcgen05.commit and hands finished accumulators to the
 // epilogue; warp 2 owns the TMEM allocation;
 // warps 4-7 drain TMEM (double-buffered, so the next item's MMAs overlap) with
@@ -118,10 +118,11 @@ __device__ __forceinline__ void st_release_gpu(unsigned* ptr, unsigned v) {
 // followed by the tail too). A's per-block scale (a power of two) becomes the
 // MMA's B-side scale factor: a 512-byte tile whose every 32-bit word holds the
 // group's UE8M0 bytes (byte b for block b), written by one B issuer into the
-// ring slot and moved to TMEM with one tcgen05.cp per group; the MMA of block
-// b selects byte b with its scale-factor id. Every word is the same, so the
-// factor does not depend on which TMEM lanes the MMA reads. The panel side's
-// factor is a constant 1 (0x7F), copied once per CTA. B's scale multiplies C
+// ring slot and moved to TMEM with one tcgen05.cp per group by each MMA
+// issuer (into its own columns); the MMA of block b selects byte b with its
+// scale-factor id. Every word is the same, so the factor does not depend on
+// which TMEM lanes the MMA reads. The panel side's factor is a constant 1
+// (0x7F), copied once per CTA and issuer. B's scale multiplies C
 // in the epilogue.
 template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
 struct TcCfg {
@@ -133,9 +134,10 @@ struct TcCfg {
   // takes the issuing thread ~74 cycles; doubling each block's UMMAs slowed
   // the headline plan by 17 %, while the same count at a quarter of the tensor
   // work saved 1-2 %), so two warps split each block's slices: disjoint
-  // accumulators, the same sums. e4m3 keeps one: its per-group scale-factor
-  // copy must precede the group's MMAs in one thread's issue order.
-  static constexpr int kIssuers = (kE4 || kJ < 2) ? 1 : 2;
+  // accumulators, the same sums. In e4m3 each issuer copies the scale factors
+  // into its own TMEM columns, so every copy precedes the MMAs that read it in
+  // one thread's issue order.
+  static constexpr int kIssuers = kJ < 2 ? 1 : 2;
   static constexpr int kJPer = kJ / kIssuers;         // slices per issuer
   static constexpr int kBoxBytes = 16 * 128;          // 16 rows x 128 bytes: 64 fp16 or 128 e4m3 columns
   static constexpr int kBoxCols = kE4 ? 128 : 64;
@@ -154,10 +156,11 @@ struct TcCfg {
   // e4m3, after the ring: the panel-side scale tile (512 bytes of 0x7F)
   static constexpr int kExtra = kE4 ? 512 : 0;
   static constexpr int kAccCols = kJ * BR;            // TMEM columns of one accumulator
-  // e4m3 scale factors in TMEM: 4 columns for the panel side, 4 per ring slot
+  // e4m3 scale factors in TMEM, per MMA issuer i: 4 columns for the panel
+  // side (kSfaCol + 4 i), 4 per ring slot s (kSfbCol + 4 (i STAGES + s))
   static constexpr int kSfaCol = ACC * kAccCols;
-  static constexpr int kSfbCol = kSfaCol + 4;
-  static constexpr int kUsedCols = kE4 ? kSfbCol + 4 * STAGES : ACC * kAccCols;
+  static constexpr int kSfbCol = kSfaCol + 4 * kIssuers;
+  static constexpr int kUsedCols = kE4 ? kSfbCol + 4 * STAGES * kIssuers : ACC * kAccCols;
   static constexpr int kTmemCols = kUsedCols <= 32 ? 32 : kUsedCols <= 64 ? 64 : kUsedCols <= 128 ? 128
                                    : kUsedCols <= 256 ? 256 : 512;
   static constexpr size_t kSmem = 1024 + (size_t)STAGES * kStage + kExtra + 1024;
@@ -591,12 +594,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     // block; each commits its own MMAs to the slot, accumulator and done
     // barriers, which expect one commit per issuer.
     if (lane == 0) {
-      const int jb = warp == 1 ? 0 : Cfg::kJPer;
+      const int mi = warp == 1 ? 0 : 1;
+      const int jb = mi * Cfg::kJPer;
+      const uint32_t sfa = tmem + Cfg::kSfaCol + 4 * mi;
       uint32_t gs = 0, it = 0;
       bool failed = false;
       if constexpr (Cfg::kE4)   // the panel side's scale factors: 1.0 for every row
-        tmem_cp_32x128b_x4(tmem + Cfg::kSfaCol,
-                           smem_desc(smem_u32(smem + (size_t)STAGES * Cfg::kStage), 128, 128, kLayoutNone));
+        tmem_cp_32x128b_x4(sfa, smem_desc(smem_u32(smem + (size_t)STAGES * Cfg::kStage), 128, 128, kLayoutNone));
       for (;; ++it) {
         int item, start, end;
         if (!read_item(it, &item, &start, &end, 8u) || item < 0) break;
@@ -619,7 +623,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           const uint32_t a_slot = smem_u32(smem + (size_t)s * Cfg::kStage);
           const uint32_t b_slot = a_slot + Cfg::kAStage;
           // e4m3: the group's scale factors into the slot's TMEM columns, ahead of its MMAs
-          const uint32_t sfb = tmem + Cfg::kSfbCol + (uint32_t)(s * 4);
+          const uint32_t sfb = tmem + Cfg::kSfbCol + (uint32_t)((mi * STAGES + s) * 4);
           if constexpr (Cfg::kE4)
             tmem_cp_32x128b_x4(sfb, smem_desc(a_slot + Cfg::kScaleOff, 128, 128, kLayoutNone));
           for (int b = 0; b < n; ++b) {
@@ -635,8 +639,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
               for (int jj = 0; jj < Cfg::kJPer; ++jj) {
                 const int j = jb + jj;
                 const uint64_t pan = smem_desc(b_addr + j * Cfg::kSliceBytes, 1024, 1024, kLayoutSW128);
-                umma_mxf8_scaled(d0 + j * BR, pan, blk_d, Cfg::kIdesc | ((uint32_t)b << 4), tmem + Cfg::kSfaCol,
-                                 sfb, accum);
+                umma_mxf8_scaled(d0 + j * BR, pan, blk_d, Cfg::kIdesc | ((uint32_t)b << 4), sfa, sfb, accum);
               }
               continue;
             }
