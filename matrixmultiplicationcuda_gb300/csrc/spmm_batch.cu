@@ -66,7 +66,7 @@ struct RingRec {
 };
 static_assert(sizeof(RingRec) == 64, "ring record");
 
-constexpr int kBatchThreads = 320;   // 10 warps, the roles of the single-product pipeline
+constexpr int kBatchThreads = 352;   // 11 warps, the roles of the single-product pipeline
 constexpr int kMaxBR = 64, kMaxNT = 256;
 
 template <int STAGES, int G>
@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
   using Cfg = BatchCfg<STAGES, G>;
   constexpr int kQ = Cfg::kQ;
   constexpr int kBIssuers = 4;
+  constexpr int kIssuers = 2;   // UMMA issuers: warp 1 (slice 0) and warp 10 (slice 1)
   // kind::f16 instruction descriptor without N: D f32, A MN-major, B K-major, M = 128
   constexpr uint32_t kIdescBase = (1u << 4) | ((BF16 ? 1u : 0u) << 7) | ((BF16 ? 1u : 0u) << 10) |
                                   (1u << 15) | ((uint32_t)(128 >> 4) << 24);
@@ -106,16 +107,16 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
   if (threadIdx.x == 32) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, kIssuers);   // each MMA issuer's commit
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tfull0 + 8 * b, kIssuers);
       mbar_init(tempty0 + 8 * b, 4);
     }
-    mbar_init(done_bar, 1);
+    mbar_init(done_bar, kIssuers);
     for (int q = 0; q < kQ; ++q) {
       mbar_init(qfull0 + 8 * q, 1);
-      mbar_init(qempty0 + 8 * q, 1 + kBIssuers + 4);   // MMA, B issuers, epilogue warps
+      mbar_init(qempty0 + 8 * q, kIssuers + kBIssuers + 4);   // MMA issuers, B issuers, epilogue warps
     }
     fence_mbar_init();
   }
@@ -283,9 +284,14 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
         }
       }
     }
-  } else if (warp == 1) {
-    // ------------------------------ MMA issuer -----------------------------------
+  } else if (warp == 1 || warp == 10) {
+    // ------------------------------ MMA issuers ----------------------------------
+    // Warp 1 issues slice 0 of every block and warp 10 slice 1 of a 256-column
+    // item (disjoint accumulators; for a 128-column item it only commits): one
+    // thread's UMMA issue rate is close to the critical path. Each commits to
+    // the slot, accumulator and done barriers, which expect one commit per issuer.
     if (lane == 0) {
+      const int mi = warp == 1 ? 0 : 1;
       uint32_t gs = 0, it = 0;
       bool failed = false;
       for (;; ++it) {
@@ -321,9 +327,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
             const uint32_t b_addr = b_slot + b * Cfg::kPanelBytes;
             const uint64_t blk = smem_desc(a_slot + b * bR * 32, 16, 256, kLayoutSW32);
             const uint32_t accum = (j0 + b != rec.start) ? 1u : 0u;
-            for (int j = 0; j < J; ++j) {
-              const uint64_t pan = smem_desc(b_addr + j * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
-              umma_f16(d0 + j * bR, pan, blk, idesc, accum);
+            if (mi < J) {
+              const uint64_t pan = smem_desc(b_addr + mi * 2 * Cfg::kBoxBytes, 2048, 1024, kLayoutSW128);
+              umma_f16(d0 + mi * bR, pan, blk, idesc, accum);
             }
           }
           umma_commit(empty0 + 8 * s);
@@ -399,8 +405,8 @@ struct BatchEntry {
   BatchEntry{ST, G, BF, &k_bcsr_tc_batch<ST, G, BF>, BatchCfg<ST, G>::kSmem}
 // (ring depth in groups, blocks per group); the first entry per type is the default.
 // All three hold eight blocks in flight; two groups of four take half the barrier
-// round trips of four groups of two and ran the 64-product uneven batch 6 % faster
-// (199 against 215 us cold, 194 against 211 us back to back).
+// round trips of four groups of two and ran the 64-product uneven batch faster
+// (187 against 192 us cold, 183 against 188 us back to back, two MMA issuers).
 const BatchEntry kBatchEntries[] = {
     SPMM_BATCH_ENTRY(2, 4, false), SPMM_BATCH_ENTRY(4, 2, false), SPMM_BATCH_ENTRY(8, 1, false),
     SPMM_BATCH_ENTRY(2, 4, true),  SPMM_BATCH_ENTRY(4, 2, true),  SPMM_BATCH_ENTRY(8, 1, true),
