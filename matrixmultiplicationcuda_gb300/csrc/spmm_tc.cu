@@ -507,6 +507,14 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           // groups it has no block in could fall two phases behind and miss a
           // parity flip.) Issuer 0 copies into every group, and so does the
           // e4m3 scale writer (its arrival is part of every group's full barrier).
+          // The parity test is only valid when group gs - 2 * STAGES has been
+          // consumed (otherwise a stale parity reads as free). Consumption is in
+          // order, so the wait in an issuer's previous group covers it as long as
+          // that group is at most STAGES groups back: issuers skip only an item's
+          // last, partial group, and the lead publishes an item once the group
+          // 2 * STAGES before its first has been consumed (claim_ahead = STAGES - 1).
+          // (Rotating the block-to-issuer map over groups of fewer than four
+          // blocks breaks this and was measured to corrupt a slot.)
           const bool writes = bidx < n || (Cfg::kE4 && bidx == kScaleWriter);
           int bad = 0;
           if (lane == 0 && writes && gs >= (uint32_t)STAGES &&
