@@ -17,7 +17,7 @@
 //   spmm_nvbench [--preset c1|c2|c3|c4|launch|compare|hybrid|all] [--tuning default,model,plan,sweep]
 //                [--min-samples 20] [--min-time 0.2] [--max-time 2]
 //                [--csv FILE] [--json FILE] [--model FILE] [--peaks FILE]
-//                [--filter SUBSTRING] [--no-check]
+//                [--filter SUBSTRING] [--no-check] [--flush write|clean]
 //
 // Presets (seeded synthetic inputs):
 //   c1  A 1024^2, 16x16 blocks, the reference generator's blockrandom pattern
@@ -39,6 +39,11 @@
 //       BCSR pipeline with every block stored, the native dense GEMM, and
 //       cuBLAS GemmEx.
 //   hybrid  the hybrid BCSR + CSR product across density thresholds.
+//
+// --flush clean: after the 256 MB write, read a second 256 MB buffer through
+// L2 before each sample. The write alone leaves L2 full of dirty lines, and
+// the timed launch pays for writing them back (~2 us on an empty kernel here);
+// after the read L2 holds clean lines and the launch is cold without that.
 //
 // Tunings: default (the library's choice), model (the cost model's pick from
 // the tuner table; a plan entry is built once and its runs are timed), plan
@@ -96,6 +101,10 @@ struct Options {
   double min_time = 0.2, max_time = 2.0;
   std::string csv, json, model, peaks, filter;
   bool check = true;
+  // cold-L2 method: false = write 256 MB before each sample (L2 is left full
+  // of dirty lines, which the timed launch then writes back); true = the same
+  // write, then a read of a second 256 MB buffer (L2 holds clean lines)
+  bool clean_flush = false;
 };
 
 struct Peaks {
@@ -344,9 +353,23 @@ struct Sample {
   int samples = 0;
 };
 
+// Reads n 16-byte words through L2 (the clean flush's second pass).
+__global__ void k_read_through_l2(const int4* __restrict__ p, size_t n, int* sink) {
+  int acc = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int4 v = __ldcg(p + i);
+    acc ^= v.x ^ v.w;
+  }
+  if (acc == 0x7fffffff) *sink = acc;   // keeps the loads; the flush buffer never holds this
+}
+
+__global__ void k_empty_launch() {}
+
 struct Timer {
   cudaEvent_t e0, e1;
   void* flush = nullptr;
+  void* flush2 = nullptr;
+  int* sink = nullptr;
   size_t flush_bytes = 256u << 20;
   Timer() {
     CK(cudaEventCreate(&e0));
@@ -357,6 +380,19 @@ struct Timer {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(flush);
+    cudaFree(flush2);
+    cudaFree(sink);
+  }
+  void flush_l2(bool clean, int k) {
+    CK(cudaMemsetAsync(flush, k & 0xff, flush_bytes, nullptr));
+    if (!clean) return;
+    if (!flush2) {
+      CK(cudaMalloc(&flush2, flush_bytes));
+      CK(cudaMemset(flush2, 0, flush_bytes));
+      CK(cudaMalloc(&sink, sizeof(int)));
+    }
+    k_read_through_l2<<<1216, 256>>>(static_cast<const int4*>(flush2), flush_bytes / 16, sink);
+    CK(cudaGetLastError());
   }
   template <class F>
   Sample measure(F&& run, const Options& o) {
@@ -365,7 +401,7 @@ struct Timer {
     std::vector<double> t;
     double total = 0;
     for (int k = 0;; ++k) {
-      CK(cudaMemsetAsync(flush, k & 0xff, flush_bytes, nullptr));
+      flush_l2(o.clean_flush, k);
       CK(cudaEventRecord(e0, nullptr));
       run();
       CK(cudaEventRecord(e1, nullptr));
@@ -429,6 +465,9 @@ class Runner {
       std::fprintf(stderr, "no cost model (%s): model tuning falls back to the sweep\n", spmm_last_error());
       model_ = nullptr;
     }
+  }
+  Sample time_empty() {
+    return timer_.measure([] { k_empty_launch<<<1, 32>>>(); }, o_);
   }
   ~Runner() {
     if (model_) spmm_cost_model_destroy(model_);
@@ -912,10 +951,17 @@ int main(int argc, char** argv) {
       o.filter = next();
     } else if (a == "--no-check") {
       o.check = false;
+    } else if (a == "--flush") {
+      const std::string f = next();
+      if (f != "write" && f != "clean") {
+        std::fprintf(stderr, "--flush takes write or clean\n");
+        return 1;
+      }
+      o.clean_flush = f == "clean";
     } else {
       std::fprintf(stderr, "usage: spmm_nvbench [--preset c1,c2,c3,c4|all] [--tuning default,model,plan,sweep] "
                            "[--min-samples N] [--min-time S] [--max-time S] [--csv F] [--json F] [--model F] "
-                           "[--peaks F] [--filter S] [--no-check]\n");
+                           "[--peaks F] [--filter S] [--no-check] [--flush write|clean]\n");
       return a == "--help" || a == "-h" ? 0 : 1;
     }
   }
@@ -923,8 +969,9 @@ int main(int argc, char** argv) {
   CK(cudaGetDeviceProperties(&prop, 0));
   Runner run(o);
   std::printf("# spmm_nvbench on %s (%d SMs); peaks (%s): HBM %.0f GB/s, tensor %.0f TFLOP/s; cold L2 "
-              "(256 MB written before each sample)\n",
-              prop.name, prop.multiProcessorCount, run.peaks().source.c_str(), run.peaks().hbm_gbs, run.peaks().tflops);
+              "(256 MB written before each sample%s)\n",
+              prop.name, prop.multiProcessorCount, run.peaks().source.c_str(), run.peaks().hbm_gbs, run.peaks().tflops,
+              o.clean_flush ? ", then a second 256 MB buffer read, so L2 holds clean lines" : "");
   for (const std::string& p : o.presets) {
     if (p == "c1") {
       run.header("c1: A 1024^2, 16x16 blocks, reference blockrandom 10 %, N 1024");
@@ -960,6 +1007,12 @@ int main(int argc, char** argv) {
                         "A 16384^2, 64x16 blocks, random 2 %, N 512");
     } else if (p == "hybrid") {
       run.hybrid_bench();
+    } else if (p == "floor") {
+      // the timing floor of this method: an empty kernel, measured like every row
+      const Sample f = run.time_empty();
+      std::printf("\n## floor: an empty kernel timed like every row\n\n| kernel | mean | median | samples |\n"
+                  "|---|---|---|---|\n| empty, <<<1, 32>>> | %.2f us | %.2f us | %d |\n",
+                  f.mean_us, f.median_us, f.samples);
     } else if (p == "launch") {
       std::printf("\n## launch: host time per call, back-to-back launches (L2 warm)\n\n");
       std::printf("| product | PDL | host per call | GPU per launch | TFLOP/s |\n|---|---|---|---|---|\n");

@@ -108,3 +108,17 @@ def test_preset_harness_c1(tmp_path):
     assert states and all(s["M"] == 1024 and s["mean_us"] > 0 for s in states)
     # the harness's own sampled check against an FP64 host product (fp16 bar 2e-3)
     assert all(0 <= s["max_rel_err"] <= 2e-3 for s in states), states
+
+
+def test_preset_floor_and_clean_flush(tmp_path):
+    """The empty-kernel floor and C1 under the clean cold-L2 method (a second
+    256 MB buffer read after the 256 MB write) run and pass the harness's check."""
+    exe = os.path.join(LIBDIR, "spmm_nvbench")
+    out = tmp_path / "clean.json"
+    r = subprocess.run([exe, "--preset", "floor,c1", "--tuning", "default", "--flush", "clean", "--min-samples", "5",
+                        "--min-time", "0.01", "--json", str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "empty, <<<1, 32>>>" in r.stdout and "second 256 MB buffer read" in r.stdout
+    import json
+    states = json.load(open(out))["states"]
+    assert states and all(s["M"] == 1024 and 0 <= s["max_rel_err"] <= 2e-3 for s in states), states

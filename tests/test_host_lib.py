@@ -223,7 +223,10 @@ def test_harness_built_and_prints_usage():
     exe = os.path.join(os.path.dirname(m.lib_path), "spmm_nvbench")
     assert os.path.exists(exe)
     r = subprocess.run([exe, "--help"], capture_output=True, text=True, timeout=60)
-    assert r.returncode == 0 and "--preset" in r.stderr
+    assert r.returncode == 0 and "--preset" in r.stderr and "--flush write|clean" in r.stderr
+    # the cold-L2 method is checked before any device call
+    r = subprocess.run([exe, "--flush", "sometimes"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "--flush takes write or clean" in r.stderr
 
 
 @pytest.mark.parametrize("th", ["0", "0.2", "0.5", "0.65", "0.8", "1.1"])
