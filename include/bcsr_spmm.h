@@ -144,6 +144,14 @@ spmm_status sparseMatrixMulTensor_v3_launch(const int* hdr, const int* idx, cons
 spmm_status sparseMatrixMulTensor_v1_improved_launch(const int* hdr, const int* idx, const void* data,
                                                      const void* B, float* C, unsigned M, unsigned N,
                                                      unsigned K, void* stream);
+/* sparseMatrixMulTensor_option2_ldmatrix_sm80, src/cuda_kernels.cu:552-613 (16x16) */
+spmm_status sparseMatrixMulTensor_option2_ldmatrix_sm80_launch(const int* hdr, const int* idx, const void* data,
+                                                               const void* B, float* C, unsigned M, unsigned N,
+                                                               unsigned K, void* stream);
+/* sparseMatrixMulTensor1, src/cuda_kernels.cu:330-355 (16x16, square n x n
+ * matrices: M = N = K = n, the reference's parameter list plus a stream) */
+spmm_status sparseMatrixMulTensor1_launch(const int* hdr, const int* idx, const void* data, const void* B,
+                                          float* C, unsigned n, void* stream);
 /* sparseMatrixMulTensor32x16_v2, src/cuda_kernels.cu:1001-1050 (32x16) */
 spmm_status sparseMatrixMulTensor32x16_v2_launch(const int* hdr, const int* idx, const void* data,
                                                  const void* B, float* C, unsigned M, unsigned N,

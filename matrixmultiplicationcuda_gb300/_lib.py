@@ -100,6 +100,9 @@ _SIGS = {
     "sparseMatrixMulTensor32x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor64x16_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor_v2_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
+    "sparseMatrixMulTensor_option2_ldmatrix_sm80_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint,
+                                                                   c_uint, c_vp]),
+    "sparseMatrixMulTensor1_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_vp]),
     "sparseMatrixMulTensor_v3_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor_v1_improved_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),
     "sparseMatrixMulTensor32x16_v2_launch": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_uint, c_uint, c_uint, c_vp]),

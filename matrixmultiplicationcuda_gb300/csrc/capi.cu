@@ -441,7 +441,14 @@ SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_shared_launch, 32)
 SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_shared_vectorized_launch, 32)
 SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor32x16_v2_shared_vectorized_launch, 32)
 SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor64x16_v2_launch, 64)
+SPMM_VARIANT_LAUNCHER(sparseMatrixMulTensor_option2_ldmatrix_sm80_launch, 16)
 #undef SPMM_VARIANT_LAUNCHER
+// sparseMatrixMulTensor1 (src/cuda_kernels.cu:330-355) multiplies square n x n
+// matrices: its one size argument is M, N and K at once.
+spmm_status sparseMatrixMulTensor1_launch(const int* hdr, const int* idx, const void* data, const void* B, float* C,
+                                          unsigned n, void* stream) {
+  return ref_launch(16, hdr, idx, data, B, C, n, n, n, stream);
+}
 spmm_status sparseMatrixMulTensorAdaptive_launch(const int* hdr, const int* idx, const void* data,
                                                  const void* B, float* C, unsigned M, unsigned N,
                                                  unsigned colBlocksPerRow, unsigned K,

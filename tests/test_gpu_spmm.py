@@ -138,7 +138,7 @@ def test_variant_launchers_agree(dev):
 
 
 VARIANTS = {16: ["sparseMatrixMulTensor_v2_launch", "sparseMatrixMulTensor_v3_launch",
-                 "sparseMatrixMulTensor_v1_improved_launch"],
+                 "sparseMatrixMulTensor_v1_improved_launch", "sparseMatrixMulTensor_option2_ldmatrix_sm80_launch"],
             32: ["sparseMatrixMulTensor32x16_v2_launch", "sparseMatrixMulTensor32x16_shared_launch",
                  "sparseMatrixMulTensor32x16_shared_vectorized_launch",
                  "sparseMatrixMulTensor32x16_v2_shared_vectorized_launch"],
@@ -166,6 +166,23 @@ def test_named_variant_launchers(dev, bR):
         assert rc == 0, (name, m._lib.last_error())
         m.device_error_check()
         assert torch.equal(C, base), name
+
+
+def test_square_launcher_tensor1(dev):
+    """sparseMatrixMulTensor1 (src/cuda_kernels.cu:330-355) takes one size n for
+    square matrices; its launcher gives the base 16x16 launcher's result."""
+    n = 256
+    A, B, hdr, idx, data = make_problem(n, n, n, "blockrandom", 0.7, 16, 16)
+    d = [to_dev(hdr, dev), to_dev(idx, dev), to_dev(data.view(np.float16), dev), to_dev(B.view(np.float16), dev)]
+    base = torch.empty((n, n), device=dev)
+    LAUNCH[16](*d, base, n, n, n)
+    C = torch.full((n, n), float("nan"), device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    rc = m.lib().sparseMatrixMulTensor1_launch(*[ctypes.c_void_p(x.data_ptr()) for x in d + [C]], n, ctypes.c_void_p(st))
+    assert rc == 0, m._lib.last_error()
+    m.device_error_check()
+    assert torch.equal(C, base)
+    assert float(np.max(np.abs(C.cpu().numpy() - oracle.cpu_matmul_ref(A, B)))) <= 1e-2
 
 
 @pytest.mark.skipif(not oracle.ref_wmma_available(), reason="reference kernels not built")
