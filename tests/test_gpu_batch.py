@@ -179,3 +179,30 @@ def test_batch_short_rows_repeated(dev):
     m.device_error_check()
     check_fp64(probs, host, "f16", bar=1e-5)
     plan.close()
+
+
+@pytest.mark.parametrize("seed", [3, 5, 9])
+def test_batch_random_mixes(dev, seed):
+    """Seeded random batches: 1-24 products of random block height, shape,
+    structure, density and N (a multiple of 8), in fp16 or bf16, on a random
+    ring depth and column tile; two runs of one plan, each against FP64."""
+    rng = np.random.default_rng(seed)
+    name = ["f16", "bf16"][seed % 2]
+    pats = [(m.PATTERN_RANDOM, 0.0), (m.PATTERN_BAND, 4.0), (m.PATTERN_LOGNORMAL, 1.5), (m.PATTERN_BLOCKDIAG, 64.0)]
+    specs = []
+    for _ in range(int(rng.integers(1, 25))):
+        bR = int(rng.choice([16, 32, 64]))
+        pat, param = pats[int(rng.integers(len(pats)))]
+        M = int(rng.integers(1, 24)) * 64
+        K = int(rng.integers(1, 40)) * 64
+        specs.append((M, K, bR, pat, float(rng.choice([0.02, 0.1, 0.4])), param, int(rng.integers(1, 64)) * 8))
+    probs, host = build_small(dev, name, specs=specs, seed=100 * seed)
+    cfg = m.Config(stages=int(rng.choice([0, 4, 8])), n_tile=int(rng.choice([0, 128, 256])))
+    plan = m.BatchPlan(probs, cfg=cfg)
+    for _ in range(2):
+        for (_, _, C) in probs:
+            C.fill_(float("nan"))
+        plan.run()
+        m.device_error_check()
+        check_fp64(probs, host, name)
+    plan.close()

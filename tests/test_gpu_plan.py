@@ -226,6 +226,43 @@ def test_plan_inputs_ready_back_to_back(dev, pattern, density):
     plan.close()
 
 
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_plan_inputs_ready_random_chains(dev, seed):
+    """Seeded random products on a random plan entry of the tuner table (every
+    block height, random shape and N, random or log-normal rows, fp16 or bf16):
+    three problems of one structure with different B, twelve launches chained
+    with SPMM_RUN_INPUTS_READY round-robin, each C equal to the same product run
+    without the flag (integer inputs: every product exact)."""
+    from matrixmultiplicationcuda_gb300 import tuner
+    rng = np.random.default_rng(seed)
+    for _ in range(3):
+        bR = int(rng.choice([16, 32, 64]))
+        M = int(rng.integers(2, 40)) * 64
+        K = int(rng.integers(2, 40)) * 64
+        N = int(rng.integers(1, 96)) * 8
+        pattern = [m.PATTERN_RANDOM, m.PATTERN_LOGNORMAL][int(rng.integers(2))]
+        dtype = [m.DType.F16, m.DType.BF16][int(rng.integers(2))]
+        density = float(rng.choice([0.02, 0.08, 0.3]))
+        A, B0 = _int_problem(M, K, N, bR, pattern, density, int(rng.integers(1 << 20)), dev, dtype)
+        mask = tuner.supported_mask(bR, dtype, N)
+        cand = [c for ok, c in zip(mask, tuner.configs()) if ok and tuner.is_plan(c)]
+        if not cand:
+            continue
+        cfg = cand[int(rng.integers(len(cand)))]
+        plan = m.BcsrPlan(A, N, cfg)
+        Bs = [B0] + [(B0 * (s + 2)).contiguous() for s in range(2)]
+        refs = [plan.run(A, B).clone() for B in Bs]
+        Cs = [torch.full((M, N), float("nan"), dtype=torch.float32, device=dev) for _ in Bs]
+        torch.cuda.synchronize()
+        for i in range(12):
+            plan.run(A, Bs[i % 3], C=Cs[i % 3], inputs_ready=True)
+        torch.cuda.synchronize()
+        m.device_error_check()
+        for C, ref in zip(Cs, refs):
+            assert torch.equal(C, ref), (bR, M, K, N, pattern, dtype.name, density, tuner.config_name(cfg))
+        plan.close()
+
+
 def test_plan_inputs_ready_keeps_c_order(dev):
     """Two launches write the same C: the second (with the flag) starts its
     copies and MMAs while the first runs, but stores C only after the first has
