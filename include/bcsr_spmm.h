@@ -245,7 +245,15 @@ spmm_status spmm_quantize(const float* src, size_t count, spmm_dtype dtype, int 
  * problems[i] describes one product; all must share dtype (F16 or BF16).
  * The launch walks one work queue of (problem, block row, column tile) items,
  * heaviest first. `plan` is an opaque host handle built once per batch
- * (it owns a device copy of the problem table and the ordered queue). */
+ * (it owns a device copy of the problem table and the ordered queue).
+ * A 16- or 32-row problem (M a multiple of 64) whose block rows share most of
+ * their columns (the union of each 64 rows' columns holds at most 60 % of the
+ * blocks, as in band and block-diagonal structures) runs stacked, as a
+ * per-matrix plan runs it: 64-row blocks over that union, zeros where a row
+ * has no block. Each spmm_batch_run then first copies the stacked problems'
+ * values into the plan's stacked blocks (one small kernel for all of them),
+ * then launches the batch. Such a problem's column indices must stay those
+ * the plan was built from; its values may change between runs. */
 typedef struct spmm_problem {
   spmm_bcsr_desc A;
   spmm_dense_desc B;
@@ -257,6 +265,8 @@ typedef struct spmm_batch_plan spmm_batch_plan;
 spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count,
                                    const spmm_config* cfg, spmm_batch_plan** plan_out);
 spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream);
+/* Items of the launch, and problems run stacked (no counterpart in the reference). */
+spmm_status spmm_batch_plan_info(const spmm_batch_plan* plan, int* items, int* stacked_problems);
 spmm_status spmm_batch_plan_destroy(spmm_batch_plan* plan);
 
 /* ---- hybrid BCSR + CSR (HCSRMatrix, formats/HCSRMatrix.cpp:10-36) -------------

@@ -120,6 +120,7 @@ _SIGS = {
     "spmm_quantize": (c_int, [c_vp, c_size, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
     "spmm_batch_plan_create": (c_int, [ctypes.POINTER(Problem), c_int, ctypes.POINTER(Config), ctypes.POINTER(c_vp)]),
     "spmm_batch_run": (c_int, [c_vp, c_vp]),
+    "spmm_batch_plan_info": (c_int, [c_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
     "spmm_batch_plan_destroy": (c_int, [c_vp]),
     "spmm_debug_wait_timeout": (c_int, [c_ull, c_vp]),
     "spmm_bcsr_mm_noalloc": (c_int, [ctypes.POINTER(BcsrDesc), ctypes.POINTER(DenseDesc), c_int, c_vp,

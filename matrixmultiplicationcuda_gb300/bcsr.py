@@ -423,6 +423,12 @@ class BatchPlan:
     def run(self, stream=None):
         check(lib().spmm_batch_run(self._h, stream_handle(stream)))
 
+    def info(self):
+        """(items of the launch, problems run stacked into 64-row blocks)."""
+        n, st = ctypes.c_int(), ctypes.c_int()
+        check(lib().spmm_batch_plan_info(self._h, ctypes.byref(n), ctypes.byref(st)))
+        return n.value, st.value
+
     def close(self):
         if self._h:
             lib().spmm_batch_plan_destroy(self._h)

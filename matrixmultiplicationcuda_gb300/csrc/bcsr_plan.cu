@@ -123,6 +123,15 @@ bool build_stack(const int* rp, const int* ci, int MB, int st, std::vector<int>*
   return true;
 }
 
+}  // namespace
+
+bool stack_structure_host(const int* rp, const int* ci, int MB, int st, std::vector<int>* srp, std::vector<int>* sci,
+                          std::vector<int>* smap) {
+  return build_stack(rp, ci, MB, st, srp, sci, smap);
+}
+
+namespace {
+
 struct Item {
   int4 d;    // {block row, column tile, first block, end block}
   int pair;  // -1, or 128 * group + part

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <string>
+#include <vector>
 #include "../../include/bcsr_spmm.h"
 
 namespace spmm {
@@ -113,6 +114,13 @@ bool tc64_supported(int bR, spmm_dtype dtype, int N, const spmm_config& cfg);
 int mma_default_nt(int bR, spmm_dtype dtype, int N);   // the column tile spmm_bcsr_mm picks by default
 
 unsigned long long wait_limit_ns();              // bounded-wait limit for device waits
+
+// The stacked structure of 16- or 32-row blocks (bcsr_plan.cu): each group of
+// `st` block rows becomes one 64-row row over the sorted union of their block
+// columns; smap holds, per stacked block and member row, the source block or
+// -1. False when a row repeats a column.
+bool stack_structure_host(const int* rp, const int* ci, int MB, int st, std::vector<int>* srp, std::vector<int>* sci,
+                          std::vector<int>* smap);
 
 // row_ptr[0] = 0, row_ptr[i + 1] = counts[0] + ... + counts[i] (one CTA, asynchronous).
 spmm_status scan_counts(const int* counts, int* row_ptr, int n, cudaStream_t s);

@@ -419,6 +419,43 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 using namespace spmm;
 
+namespace spmm {
+namespace {
+
+// One stacked problem of a batch: its values are copied into the stacked
+// 64-row blocks before every launch (members = stacked blocks x rows per
+// stack; chunks = 16-byte chunks of one source block).
+struct StackSeg {
+  const int4* src;
+  const int* map;
+  int4* dst;
+  long long first;     // first chunk of this segment in the launch's index space
+  long long count;     // members * chunks
+  int chunks;
+  int pad;
+};
+
+// One thread per 16-byte chunk of every stacked problem of the batch: chunk x
+// of member i of a segment is chunk x of source block map[i], or zeros.
+__global__ void k_batch_stack_repack(const StackSeg* __restrict__ segs, int nseg, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {   // the last segment whose first chunk is <= g
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].first <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    const StackSeg sg = segs[lo];
+    const long long x = g - sg.first;
+    const long long i = x / sg.chunks;
+    const int b = __ldg(sg.map + i);
+    sg.dst[x] = b >= 0 ? __ldg(sg.src + (long long)b * sg.chunks + (x - i * sg.chunks)) : make_int4(0, 0, 0, 0);
+  }
+}
+
+}  // namespace
+}  // namespace spmm
+
 struct spmm_batch_plan {
   int device = -1;
   int count = 0;
@@ -430,6 +467,14 @@ struct spmm_batch_plan {
   unsigned* d_queue = nullptr;
   unsigned* err = nullptr;
   unsigned long long timeout_ns = 0;
+  // 16- and 32-row problems whose block rows share most columns, stacked into
+  // 64-row blocks (as a per-matrix plan stacks them): device arrays the plan
+  // owns, the segment table, and the chunk count of the repack launch
+  std::vector<void*> owned;
+  spmm::StackSeg* d_segs = nullptr;
+  int nseg = 0;
+  long long repack_total = 0;
+  int stacked = 0;
 };
 
 namespace {
@@ -459,6 +504,8 @@ void free_plan(spmm_batch_plan* p) {
   if (p->d_probs) cudaFree(p->d_probs);
   if (p->d_items) cudaFree(p->d_items);
   if (p->d_queue) cudaFree(p->d_queue);
+  for (void* q : p->owned) cudaFree(q);
+  if (p->d_segs) cudaFree(p->d_segs);
   delete p;
 }
 
@@ -516,6 +563,8 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
   };
   std::vector<Keyed> items;
   std::vector<int> rp;
+  std::vector<StackSeg> segs;
+  cudaError_t ce = cudaSuccess;
   for (int i = 0; i < count; ++i) {
     const spmm_problem& pb = problems[i];
     const spmm_bcsr_desc& A = pb.A;
@@ -549,16 +598,68 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
     d.N = pb.N;
     d.bR = A.bR;
     d.ntp = ntp;
+    // Stacking: 16- or 32-row block rows that make up 64 rows of C are run as
+    // one 64-row row over the union of their block columns (zeros where a row
+    // has no block), when that union holds at most 60 % of the blocks: one
+    // UMMA, one B panel and one item for up to 4 blocks.
+    int bR_run = A.bR, rows_run = MB;
+    const void* vals_run = A.vals;
+    if ((A.bR == 16 || A.bR == 32) && A.M % 64 == 0 && nnzb > 0 && A.vals) {
+      std::vector<int> ci((size_t)nnzb), srp, sci, smap;
+      ce = cudaMemcpy(ci.data(), A.col_idx, sizeof(int) * nnzb, cudaMemcpyDeviceToHost);
+      if (ce != cudaSuccess) {
+        free_plan(plan);
+        return cuda_fail(ce, "reading col_idx");
+      }
+      const int stk = 64 / A.bR;
+      if (stack_structure_host(rp.data(), ci.data(), MB, stk, &srp, &sci, &smap) &&
+          (long long)sci.size() * 100 <= nnzb * 60) {
+        int* d_srp = nullptr;
+        int* d_sci = nullptr;
+        int* d_map = nullptr;
+        void* d_vals = nullptr;
+        ce = cudaMalloc(&d_srp, sizeof(int) * srp.size());
+        if (ce == cudaSuccess) plan->owned.push_back(d_srp), ce = cudaMalloc(&d_sci, sizeof(int) * sci.size());
+        if (ce == cudaSuccess) plan->owned.push_back(d_sci), ce = cudaMalloc(&d_map, sizeof(int) * smap.size());
+        if (ce == cudaSuccess) plan->owned.push_back(d_map), ce = cudaMalloc(&d_vals, sci.size() * 64 * 16 * 2);
+        if (ce == cudaSuccess) plan->owned.push_back(d_vals);
+        if (ce == cudaSuccess) ce = cudaMemcpy(d_srp, srp.data(), sizeof(int) * srp.size(), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) ce = cudaMemcpy(d_sci, sci.data(), sizeof(int) * sci.size(), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess)
+          ce = cudaMemcpy(d_map, smap.data(), sizeof(int) * smap.size(), cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) {
+          free_plan(plan);
+          return cuda_fail(ce, "setting up a stacked problem");
+        }
+        StackSeg sg;
+        sg.src = static_cast<const int4*>(A.vals);
+        sg.map = d_map;
+        sg.dst = static_cast<int4*>(d_vals);
+        sg.chunks = A.bR * 2;
+        sg.count = (long long)smap.size() * sg.chunks;
+        sg.first = plan->repack_total;
+        sg.pad = 0;
+        plan->repack_total += sg.count;
+        segs.push_back(sg);
+        plan->stacked += 1;
+        rp.assign(srp.begin(), srp.end());
+        rows_run = (int)srp.size() - 1;
+        bR_run = 64;
+        vals_run = d_vals;
+        d.col_idx = d_sci;
+        d.bR = 64;
+      }
+    }
     if (nnzb > 0) {
       const unsigned long long rows_bound =
-          std::max<unsigned long long>((unsigned long long)MB * (A.K / 16) * A.bR, 256ull);
+          std::max<unsigned long long>((unsigned long long)rows_run * (A.K / 16) * bR_run, 256ull);
       spmm_status st = rows_bound >= (1ull << 31)
                            ? fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline")
-                           : encode_tile_map_2d(&d.tmA1, CU_TENSOR_MAP_DATA_TYPE_UINT16, A.vals, 16, rows_bound,
-                                                32, 16, (uint32_t)A.bR, CU_TENSOR_MAP_SWIZZLE_32B);
+                           : encode_tile_map_2d(&d.tmA1, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals_run, 16, rows_bound,
+                                                32, 16, (uint32_t)bR_run, CU_TENSOR_MAP_SWIZZLE_32B);
       if (st == SPMM_OK)
-        st = encode_tile_map_2d(&d.tmAg, CU_TENSOR_MAP_DATA_TYPE_UINT16, A.vals, 16, rows_bound, 32, 16,
-                                (uint32_t)(e->group * A.bR), CU_TENSOR_MAP_SWIZZLE_32B);
+        st = encode_tile_map_2d(&d.tmAg, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals_run, 16, rows_bound, 32, 16,
+                                (uint32_t)(e->group * bR_run), CU_TENSOR_MAP_SWIZZLE_32B);
       d.panel3d = pb.N % 64 == 0 ? 1 : 0;
       if (st == SPMM_OK && d.panel3d &&
           encode_panel_map_3d(&d.tmB, pb.B.data, (uint64_t)pb.N, (uint64_t)A.K, (uint64_t)pb.B.ldb * 2,
@@ -575,11 +676,11 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
     const int ntiles = (pb.N + ntp - 1) / ntp;
     // cost of an item ~ bytes it moves: per block the A block and a B panel,
     // plus the C tile it writes
-    for (int r = 0; r < MB; ++r) {
+    for (int r = 0; r < rows_run; ++r) {
       const int nb = rp[r + 1] - rp[r];
       for (int t = 0; t < ntiles; ++t) {
         Keyed k;
-        k.cost = (double)nb * (A.bR * 32 + ntp * 32) + (double)A.bR * ntp * 4;
+        k.cost = (double)nb * (bR_run * 32 + ntp * 32) + (double)bR_run * ntp * 4;
         k.it = BatchItem{i, r, t, rp[r], rp[r + 1], 0, 0, 0};
         items.push_back(k);
       }
@@ -594,7 +695,17 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
   std::vector<BatchItem> flat(items.size());
   for (size_t k = 0; k < items.size(); ++k) flat[k] = items[k].it;
 
-  cudaError_t ce = cudaMalloc(&plan->d_probs, sizeof(BatchProblemDev) * probs.size());
+  if (!segs.empty()) {
+    ce = cudaMalloc(&plan->d_segs, sizeof(StackSeg) * segs.size());
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(plan->d_segs, segs.data(), sizeof(StackSeg) * segs.size(), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+      free_plan(plan);
+      return cuda_fail(ce, "setting up the stacked problems");
+    }
+    plan->nseg = (int)segs.size();
+  }
+  ce = cudaMalloc(&plan->d_probs, sizeof(BatchProblemDev) * probs.size());
   if (ce == cudaSuccess)
     ce = cudaMemcpy(plan->d_probs, probs.data(), sizeof(BatchProblemDev) * probs.size(), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMalloc(&plan->d_items, sizeof(BatchItem) * std::max<size_t>(flat.size(), 1));
@@ -619,8 +730,8 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
   if (grid > plan->n_items) grid = plan->n_items;
   plan->grid = (int)grid;
   if (std::getenv("SPMM_DEBUG"))
-    std::fprintf(stderr, "[spmm] batch problems=%d items=%d stages=%d group=%d smem=%zu grid=%d\n", count,
-                 plan->n_items, e->stages, e->group, e->smem, plan->grid);
+    std::fprintf(stderr, "[spmm] batch problems=%d stacked=%d items=%d stages=%d group=%d smem=%zu grid=%d\n",
+                 count, plan->stacked, plan->n_items, e->stages, e->group, e->smem, plan->grid);
   *plan_out = plan;
   return SPMM_OK;
 }
@@ -631,6 +742,14 @@ spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream) {
   SPMM_CUDA_TRY(cudaGetDevice(&dev));
   if (dev != plan->device) return fail(SPMM_ERR_INVALID_ARG, "plan was built on another device");
   if (plan->n_items == 0) return SPMM_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (plan->nseg > 0) {
+    // this run's values into the stacked blocks; the batch kernel waits for
+    // this launch before it reads A
+    const long long grid = std::min<long long>((plan->repack_total + 255) / 256, (long long)sm_count() * 8);
+    k_batch_stack_repack<<<(unsigned)grid, 256, 0, s>>>(plan->d_segs, plan->nseg, plan->repack_total);
+    SPMM_CUDA_TRY(cudaGetLastError());
+  }
   BatchParams p;
   p.probs = plan->d_probs;
   p.items = plan->d_items;
@@ -639,7 +758,14 @@ spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream) {
   p.err = plan->err;
   p.timeout_ns = plan->timeout_ns;
   SPMM_CUDA_TRY(launch_kernel(plan->entry->fn, dim3((unsigned)plan->grid), dim3(kBatchThreads), plan->entry->smem,
-                              static_cast<cudaStream_t>(stream), p));
+                              s, p));
+  return SPMM_OK;
+}
+
+spmm_status spmm_batch_plan_info(const spmm_batch_plan* plan, int* items, int* stacked_problems) {
+  if (!plan) return fail(SPMM_ERR_INVALID_ARG, "null plan");
+  if (items) *items = plan->n_items;
+  if (stacked_problems) *stacked_problems = plan->stacked;
   return SPMM_OK;
 }
 

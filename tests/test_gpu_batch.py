@@ -206,3 +206,36 @@ def test_batch_random_mixes(dev, seed):
         m.device_error_check()
         check_fp64(probs, host, name)
     plan.close()
+
+
+def test_batch_stacks_shared_column_problems(dev):
+    """16- and 32-row band and block-diagonal problems run stacked into 64-row
+    blocks over the union of their rows' columns; random ones and 64-row ones
+    run as they are. Every product matches FP64 over two runs, and after new
+    values are written into the stacked problems' A (the copy into the stacked
+    blocks is refreshed by every run)."""
+    specs = [
+        (1024, 1024, 16, m.PATTERN_BAND, 0.1, 6.0, 256),       # stacks
+        (1024, 1024, 32, m.PATTERN_BLOCKDIAG, 0.0, 128.0, 128),  # stacks
+        (1024, 2048, 16, m.PATTERN_RANDOM, 0.05, 0.0, 512),     # union ~ all blocks: does not
+        (512, 512, 64, m.PATTERN_BAND, 0.1, 4.0, 256),         # 64-row: as it is
+        (960, 1024, 16, m.PATTERN_BLOCKDIAG, 0.0, 64.0, 200),   # stacks, ragged N
+    ]
+    probs, host = build_small(dev, "f16", specs=specs, seed=77)
+    plan = m.BatchPlan(probs)
+    assert plan.info()[1] == 3
+    for _ in range(2):
+        for (_, _, C) in probs:
+            C.fill_(float("nan"))
+        plan.run()
+        m.device_error_check()
+        check_fp64(probs, host, "f16")
+    # new values in place (same structure): the next run multiplies them
+    for k, ((A, B, C), (rp, ci, vals, Bf, bR)) in enumerate(zip(probs, host)):
+        v2 = m.gen_values(len(ci), bR, 16, m.DIST_UNIFORM, seed=900 + k)
+        A.vals.copy_(torch.from_numpy(v2).to(dev).half())
+        host[k] = (rp, ci, v2, Bf, bR)
+    plan.run()
+    m.device_error_check()
+    check_fp64(probs, host, "f16")
+    plan.close()
