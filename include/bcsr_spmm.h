@@ -250,10 +250,11 @@ spmm_status spmm_quantize(const float* src, size_t count, spmm_dtype dtype, int 
  * their columns (the union of each 64 rows' columns holds at most 60 % of the
  * blocks, as in band and block-diagonal structures) runs stacked, as a
  * per-matrix plan runs it: 64-row blocks over that union, zeros where a row
- * has no block. Each spmm_batch_run then first copies the stacked problems'
- * values into the plan's stacked blocks (one small kernel for all of them),
- * then launches the batch. Such a problem's column indices must stay those
- * the plan was built from; its values may change between runs. */
+ * has no block. The launch assembles each stacked block in shared memory
+ * from its member blocks, read from the problem's own values (rows with no
+ * block read zeros), so a run takes the current values and needs no copy.
+ * Such a problem's column indices must stay those the plan was built from;
+ * its values may change between runs. */
 typedef struct spmm_problem {
   spmm_bcsr_desc A;
   spmm_dense_desc B;

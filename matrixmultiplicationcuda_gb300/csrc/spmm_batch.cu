@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #include "internal.h"
 #include "ptx.cuh"
@@ -33,13 +34,19 @@ namespace spmm {
 namespace {
 
 struct alignas(64) BatchProblemDev {
-  CUtensorMap tmA1;   // A values as [rows x 16], box = one block
-  CUtensorMap tmAg;   // same tensor, box = G blocks
+  CUtensorMap tmA1;   // A values as [rows x 16], box = one block (a stacked problem: one member block)
+  CUtensorMap tmAg;   // same tensor, box = G blocks (not used by a stacked problem)
   CUtensorMap tmB;    // B panels: 3-D {64, K, N/64} box {64, 16, ntp/64}, or 2-D box {64, 16}
   const int* col_idx;
   float* C;
   long long ldc;
   int N, bR, ntp, panel3d;
+  // stacked problem (stk > 1): its 64-row blocks are assembled in shared
+  // memory from stk member blocks of mbR rows each; smap holds, per stacked
+  // block and member, the source block of A or -1 (rows of zeros, loaded
+  // from row oob_row, past the end of A's tensor map)
+  const int* smap;
+  int stk, mbR, oob_row, pad;
 };
 
 struct BatchItem {
@@ -59,7 +66,7 @@ struct BatchParams {
 // One entry of the item ring (64 bytes): the item plus the problem fields the
 // consumer roles need. prob < 0 ends the stream.
 struct RingRec {
-  int prob, br, nt, start, end, bR, ntp, N, panel3d, pad;
+  int prob, br, nt, start, end, bR, ntp, N, panel3d, stk;
   const int* col_idx;
   float* C;
   long long ldc;
@@ -174,11 +181,12 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
         r.ntp = __ldg(&pr->ntp);
         r.N = __ldg(&pr->N);
         r.panel3d = __ldg(&pr->panel3d);
+        r.stk = __ldg(&pr->stk);
         r.col_idx = pr->col_idx;
         r.C = pr->C;
         r.ldc = __ldg(&pr->ldc);
         if (r.end > r.start) {
-          tma_prefetch_desc(&pr->tmAg);
+          if (r.stk <= 1) tma_prefetch_desc(&pr->tmAg);
           tma_prefetch_desc(&pr->tmB);
         }
       };
@@ -213,7 +221,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
           mbar_arrive_expect_tx(fb, (uint32_t)n * blk_bytes);
           uint8_t* a_dst = smem + (size_t)s * Cfg::kStage;
           const int y0 = j0 * bR;
-          if (n == G) {
+          if (cur.stk > 1) {
+            // a stacked problem's member blocks are copied by the B issuers
+          } else if (n == G) {
             tma_tile_2d_g2s(smem_u32(a_dst), &pr->tmAg, 0, y0, fb, pol_a);
           } else {
             for (int b = 0; b < n; ++b)
@@ -243,46 +253,85 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_bcsr_tc_batch(const BatchP
     for (uint32_t it = 0; !failed; ++it) {
       RingRec rec;
       if (!read_rec_warp(it, rec, 4u) || rec.prob < 0) break;
-      const CUtensorMap* tmB = &p.probs[rec.prob].tmB;
+      const BatchProblemDev* pr = p.probs + rec.prob;
+      const CUtensorMap* tmB = &pr->tmB;
       const int boxes = rec.ntp / 64;
-      int mycol = lane < rec.end - rec.start ? __ldg(rec.col_idx + rec.start + lane) : 0;
-      for (int base = rec.start; base < rec.end && !failed; base += 32) {
-        const int cnt = min(32, rec.end - base);
-        const int cur = mycol;
-        if (base + 32 < rec.end) mycol = lane < rec.end - base - 32 ? __ldg(rec.col_idx + base + 32 + lane) : 0;
-        for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
-          const int n = min(G, cnt - i0);
-          const int s = (int)(gs % STAGES);
-          // Wait for the slot only in groups this issuer copies into: such a
-          // group cannot be released without its bytes, so the slot's empty
-          // barrier is at most one phase ahead. (An issuer that also waited in
-          // groups it has no block in could fall two phases behind and miss a
-          // parity flip.)
-          int bad = 0;
-          if (lane == 0 && bidx < n && gs >= (uint32_t)STAGES &&
-              !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
-            atomicOr(p.err, 4u);
-            bad = 1;
-          }
-          failed = __shfl_sync(0xffffffffu, bad, 0);
-          if (failed) break;
-          uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
-          for (int b = bidx; b < n; b += kBIssuers) {
-            const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
-            if (lane == 0) {
-              const uint32_t fb = full0 + 8 * s;
-              uint8_t* b_dst = b_dst0 + (size_t)b * Cfg::kPanelBytes;
-              if (rec.panel3d) {
-                tma_tile_3d_g2s(smem_u32(b_dst), tmB, 0, col * 16, rec.nt * boxes, fb, pol_b);
-              } else {
-                for (int bx = 0; bx < boxes; ++bx)
-                  tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), tmB, rec.nt * rec.ntp + bx * 64,
-                                  col * 16, fb, pol_b);
+      // One pass over the item's blocks. A stacked problem (stk > 1) also
+      // copies, per stacked block, its stk member blocks of mbR rows from the
+      // source blocks its map names (-1: a box past the end of A, which reads
+      // zeros). The two cases are separate instantiations, so the plain path
+      // carries none of the member bookkeeping.
+      auto issue_blocks = [&](auto stacked_tag) {
+        constexpr bool kStacked = decltype(stacked_tag)::value;
+        const int stk = rec.stk;
+        const int* smap = kStacked ? pr->smap : nullptr;
+        const int mbR = kStacked ? __ldg(&pr->mbR) : 0, oob = kStacked ? __ldg(&pr->oob_row) : 0;
+        auto load_members = [&](int j, int (&mm)[4]) {
+#pragma unroll
+          for (int t = 0; t < 4; ++t) mm[t] = (t < stk && j < rec.end) ? __ldg(smap + (long long)j * stk + t) : -1;
+        };
+        int mym[4] = {-1, -1, -1, -1};
+        if constexpr (kStacked) load_members(rec.start + lane, mym);
+        int mycol = lane < rec.end - rec.start ? __ldg(rec.col_idx + rec.start + lane) : 0;
+        for (int base = rec.start; base < rec.end && !failed; base += 32) {
+          const int cnt = min(32, rec.end - base);
+          const int cur = mycol;
+          int curm[4] = {mym[0], mym[1], mym[2], mym[3]};
+          if constexpr (kStacked)
+            if (base + 32 < rec.end) load_members(base + 32 + lane, mym);
+          if (base + 32 < rec.end) mycol = lane < rec.end - base - 32 ? __ldg(rec.col_idx + base + 32 + lane) : 0;
+          for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
+            const int n = min(G, cnt - i0);
+            const int s = (int)(gs % STAGES);
+            // Wait for the slot only in groups this issuer copies into: such a
+            // group cannot be released without its bytes, so the slot's empty
+            // barrier is at most one phase ahead. (An issuer that also waited in
+            // groups it has no block in could fall two phases behind and miss a
+            // parity flip.)
+            int bad = 0;
+            if (lane == 0 && bidx < n && gs >= (uint32_t)STAGES &&
+                !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
+              atomicOr(p.err, 4u);
+              bad = 1;
+            }
+            failed = __shfl_sync(0xffffffffu, bad, 0);
+            if (failed) break;
+            uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
+            for (int b = bidx; b < n; b += kBIssuers) {
+              const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
+              int src[4] = {-1, -1, -1, -1};
+              if constexpr (kStacked) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) src[t] = __shfl_sync(0xffffffffu, curm[t], i0 + b);
+              }
+              if (lane == 0) {
+                const uint32_t fb = full0 + 8 * s;
+                if constexpr (kStacked) {
+                  // the stacked 64-row block: member t's rows at t * mbR
+                  uint8_t* a_dst = smem + (size_t)s * Cfg::kStage + (size_t)b * 64 * 32;
+#pragma unroll
+                  for (int t = 0; t < 4; ++t)
+                    if (t < stk)
+                      tma_tile_2d_g2s(smem_u32(a_dst + t * mbR * 32), &pr->tmA1, 0, src[t] >= 0 ? src[t] * mbR : oob,
+                                      fb, pol_b);
+                }
+                uint8_t* b_dst = b_dst0 + (size_t)b * Cfg::kPanelBytes;
+                if (rec.panel3d) {
+                  tma_tile_3d_g2s(smem_u32(b_dst), tmB, 0, col * 16, rec.nt * boxes, fb, pol_b);
+                } else {
+                  for (int bx = 0; bx < boxes; ++bx)
+                    tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), tmB, rec.nt * rec.ntp + bx * 64,
+                                    col * 16, fb, pol_b);
+                }
               }
             }
           }
         }
-      }
+      };
+      if (rec.stk > 1)
+        issue_blocks(std::true_type{});
+      else
+        issue_blocks(std::false_type{});
     }
   } else if (warp == 1 || warp == 10) {
     // ------------------------------ MMA issuers ----------------------------------
@@ -403,10 +452,12 @@ struct BatchEntry {
 };
 #define SPMM_BATCH_ENTRY(ST, G, BF) \
   BatchEntry{ST, G, BF, &k_bcsr_tc_batch<ST, G, BF>, BatchCfg<ST, G>::kSmem}
-// (ring depth in groups, blocks per group); the first entry per type is the default.
-// All three hold eight blocks in flight; two groups of four take half the barrier
-// round trips of four groups of two and ran the 64-product uneven batch faster
-// (187 against 192 us cold, 183 against 188 us back to back, two MMA issuers).
+// (ring depth in groups, blocks per group); the first entry per type is the default,
+// and the 4-stage one the default of a batch with stacked problems. All three hold
+// eight blocks in flight; two groups of four take half the barrier round trips of
+// four groups of two and ran the 64-product uneven batch faster with stacking off
+// (188 against 192 us); with stacking on, four groups of two ran it in 151 against
+// 157 us (and a second seed's 64 products in 257 against 274 us).
 const BatchEntry kBatchEntries[] = {
     SPMM_BATCH_ENTRY(2, 4, false), SPMM_BATCH_ENTRY(4, 2, false), SPMM_BATCH_ENTRY(8, 1, false),
     SPMM_BATCH_ENTRY(2, 4, true),  SPMM_BATCH_ENTRY(4, 2, true),  SPMM_BATCH_ENTRY(8, 1, true),
@@ -418,43 +469,6 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 }  // namespace spmm
 
 using namespace spmm;
-
-namespace spmm {
-namespace {
-
-// One stacked problem of a batch: its values are copied into the stacked
-// 64-row blocks before every launch (members = stacked blocks x rows per
-// stack; chunks = 16-byte chunks of one source block).
-struct StackSeg {
-  const int4* src;
-  const int* map;
-  int4* dst;
-  long long first;     // first chunk of this segment in the launch's index space
-  long long count;     // members * chunks
-  int chunks;
-  int pad;
-};
-
-// One thread per 16-byte chunk of every stacked problem of the batch: chunk x
-// of member i of a segment is chunk x of source block map[i], or zeros.
-__global__ void k_batch_stack_repack(const StackSeg* __restrict__ segs, int nseg, long long total) {
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nseg - 1;
-    while (lo < hi) {   // the last segment whose first chunk is <= g
-      const int mid = (lo + hi + 1) >> 1;
-      if (segs[mid].first <= g) lo = mid;
-      else hi = mid - 1;
-    }
-    const StackSeg sg = segs[lo];
-    const long long x = g - sg.first;
-    const long long i = x / sg.chunks;
-    const int b = __ldg(sg.map + i);
-    sg.dst[x] = b >= 0 ? __ldg(sg.src + (long long)b * sg.chunks + (x - i * sg.chunks)) : make_int4(0, 0, 0, 0);
-  }
-}
-
-}  // namespace
-}  // namespace spmm
 
 struct spmm_batch_plan {
   int device = -1;
@@ -468,12 +482,9 @@ struct spmm_batch_plan {
   unsigned* err = nullptr;
   unsigned long long timeout_ns = 0;
   // 16- and 32-row problems whose block rows share most columns, stacked into
-  // 64-row blocks (as a per-matrix plan stacks them): device arrays the plan
-  // owns, the segment table, and the chunk count of the repack launch
+  // 64-row blocks (as a per-matrix plan stacks them): the device arrays of
+  // their stacked structure, which the plan owns
   std::vector<void*> owned;
-  spmm::StackSeg* d_segs = nullptr;
-  int nseg = 0;
-  long long repack_total = 0;
   int stacked = 0;
 };
 
@@ -505,7 +516,6 @@ void free_plan(spmm_batch_plan* p) {
   if (p->d_items) cudaFree(p->d_items);
   if (p->d_queue) cudaFree(p->d_queue);
   for (void* q : p->owned) cudaFree(q);
-  if (p->d_segs) cudaFree(p->d_segs);
   delete p;
 }
 
@@ -563,7 +573,15 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
   };
   std::vector<Keyed> items;
   std::vector<int> rp;
-  std::vector<StackSeg> segs;
+  // the group maps (box = G blocks) of the problems that are not stacked,
+  // encoded once the ring's group size is known
+  struct GroupMap {
+    int prob;
+    const void* vals;
+    unsigned long long rows;
+    int bR;
+  };
+  std::vector<GroupMap> group_maps;
   cudaError_t ce = cudaSuccess;
   for (int i = 0; i < count; ++i) {
     const spmm_problem& pb = problems[i];
@@ -603,7 +621,6 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
     // has no block), when that union holds at most 60 % of the blocks: one
     // UMMA, one B panel and one item for up to 4 blocks.
     int bR_run = A.bR, rows_run = MB;
-    const void* vals_run = A.vals;
     if ((A.bR == 16 || A.bR == 32) && A.M % 64 == 0 && nnzb > 0 && A.vals) {
       std::vector<int> ci((size_t)nnzb), srp, sci, smap;
       ce = cudaMemcpy(ci.data(), A.col_idx, sizeof(int) * nnzb, cudaMemcpyDeviceToHost);
@@ -614,16 +631,11 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
       const int stk = 64 / A.bR;
       if (stack_structure_host(rp.data(), ci.data(), MB, stk, &srp, &sci, &smap) &&
           (long long)sci.size() * 100 <= nnzb * 60) {
-        int* d_srp = nullptr;
         int* d_sci = nullptr;
         int* d_map = nullptr;
-        void* d_vals = nullptr;
-        ce = cudaMalloc(&d_srp, sizeof(int) * srp.size());
-        if (ce == cudaSuccess) plan->owned.push_back(d_srp), ce = cudaMalloc(&d_sci, sizeof(int) * sci.size());
+        ce = cudaMalloc(&d_sci, sizeof(int) * sci.size());
         if (ce == cudaSuccess) plan->owned.push_back(d_sci), ce = cudaMalloc(&d_map, sizeof(int) * smap.size());
-        if (ce == cudaSuccess) plan->owned.push_back(d_map), ce = cudaMalloc(&d_vals, sci.size() * 64 * 16 * 2);
-        if (ce == cudaSuccess) plan->owned.push_back(d_vals);
-        if (ce == cudaSuccess) ce = cudaMemcpy(d_srp, srp.data(), sizeof(int) * srp.size(), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) plan->owned.push_back(d_map);
         if (ce == cudaSuccess) ce = cudaMemcpy(d_sci, sci.data(), sizeof(int) * sci.size(), cudaMemcpyHostToDevice);
         if (ce == cudaSuccess)
           ce = cudaMemcpy(d_map, smap.data(), sizeof(int) * smap.size(), cudaMemcpyHostToDevice);
@@ -631,35 +643,29 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
           free_plan(plan);
           return cuda_fail(ce, "setting up a stacked problem");
         }
-        StackSeg sg;
-        sg.src = static_cast<const int4*>(A.vals);
-        sg.map = d_map;
-        sg.dst = static_cast<int4*>(d_vals);
-        sg.chunks = A.bR * 2;
-        sg.count = (long long)smap.size() * sg.chunks;
-        sg.first = plan->repack_total;
-        sg.pad = 0;
-        plan->repack_total += sg.count;
-        segs.push_back(sg);
         plan->stacked += 1;
         rp.assign(srp.begin(), srp.end());
         rows_run = (int)srp.size() - 1;
         bR_run = 64;
-        vals_run = d_vals;
         d.col_idx = d_sci;
         d.bR = 64;
+        d.smap = d_map;
+        d.stk = stk;
+        d.mbR = A.bR;
       }
     }
     if (nnzb > 0) {
+      // A's values as [rows x 16]; a stacked problem reads its member blocks
+      // (mbR rows) from the original values, and rows past rows_bound read zeros
+      const int box_rows = d.stk > 1 ? d.mbR : bR_run;
       const unsigned long long rows_bound =
-          std::max<unsigned long long>((unsigned long long)rows_run * (A.K / 16) * bR_run, 256ull);
-      spmm_status st = rows_bound >= (1ull << 31)
+          std::max<unsigned long long>((unsigned long long)MB * (A.K / 16) * A.bR, 256ull);
+      d.oob_row = (int)rows_bound;
+      spmm_status st = rows_bound >= (1ull << 31) - 64
                            ? fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline")
-                           : encode_tile_map_2d(&d.tmA1, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals_run, 16, rows_bound,
-                                                32, 16, (uint32_t)bR_run, CU_TENSOR_MAP_SWIZZLE_32B);
-      if (st == SPMM_OK)
-        st = encode_tile_map_2d(&d.tmAg, CU_TENSOR_MAP_DATA_TYPE_UINT16, vals_run, 16, rows_bound, 32, 16,
-                                (uint32_t)(e->group * bR_run), CU_TENSOR_MAP_SWIZZLE_32B);
+                           : encode_tile_map_2d(&d.tmA1, CU_TENSOR_MAP_DATA_TYPE_UINT16, A.vals, 16, rows_bound,
+                                                32, 16, (uint32_t)box_rows, CU_TENSOR_MAP_SWIZZLE_32B);
+      if (st == SPMM_OK && d.stk <= 1) group_maps.push_back(GroupMap{i, A.vals, rows_bound, A.bR});
       d.panel3d = pb.N % 64 == 0 ? 1 : 0;
       if (st == SPMM_OK && d.panel3d &&
           encode_panel_map_3d(&d.tmB, pb.B.data, (uint64_t)pb.N, (uint64_t)A.K, (uint64_t)pb.B.ldb * 2,
@@ -690,21 +696,26 @@ spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count, cons
     free_plan(plan);
     return fail(SPMM_ERR_UNSUPPORTED, "batched launch: too many items");
   }
+  // A batch with stacked problems defaults to four groups of two: each stacked
+  // block is up to four member copies, and the deeper ring keeps more of them
+  // in flight.
+  if (c.stages == 0 && plan->stacked > 0)
+    for (const BatchEntry& x : kBatchEntries)
+      if (x.bf16 == e->bf16 && x.stages == 4) e = &x;
+  plan->entry = e;
+  for (const GroupMap& g : group_maps) {
+    spmm_status st = encode_tile_map_2d(&probs[g.prob].tmAg, CU_TENSOR_MAP_DATA_TYPE_UINT16, g.vals, 16, g.rows, 32,
+                                        16, (uint32_t)(e->group * g.bR), CU_TENSOR_MAP_SWIZZLE_32B);
+    if (st != SPMM_OK) {
+      free_plan(plan);
+      return st;
+    }
+  }
   std::stable_sort(items.begin(), items.end(), [](const Keyed& a, const Keyed& b) { return a.cost > b.cost; });
   plan->n_items = (int)items.size();
   std::vector<BatchItem> flat(items.size());
   for (size_t k = 0; k < items.size(); ++k) flat[k] = items[k].it;
 
-  if (!segs.empty()) {
-    ce = cudaMalloc(&plan->d_segs, sizeof(StackSeg) * segs.size());
-    if (ce == cudaSuccess)
-      ce = cudaMemcpy(plan->d_segs, segs.data(), sizeof(StackSeg) * segs.size(), cudaMemcpyHostToDevice);
-    if (ce != cudaSuccess) {
-      free_plan(plan);
-      return cuda_fail(ce, "setting up the stacked problems");
-    }
-    plan->nseg = (int)segs.size();
-  }
   ce = cudaMalloc(&plan->d_probs, sizeof(BatchProblemDev) * probs.size());
   if (ce == cudaSuccess)
     ce = cudaMemcpy(plan->d_probs, probs.data(), sizeof(BatchProblemDev) * probs.size(), cudaMemcpyHostToDevice);
@@ -743,13 +754,6 @@ spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream) {
   if (dev != plan->device) return fail(SPMM_ERR_INVALID_ARG, "plan was built on another device");
   if (plan->n_items == 0) return SPMM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (plan->nseg > 0) {
-    // this run's values into the stacked blocks; the batch kernel waits for
-    // this launch before it reads A
-    const long long grid = std::min<long long>((plan->repack_total + 255) / 256, (long long)sm_count() * 8);
-    k_batch_stack_repack<<<(unsigned)grid, 256, 0, s>>>(plan->d_segs, plan->nseg, plan->repack_total);
-    SPMM_CUDA_TRY(cudaGetLastError());
-  }
   BatchParams p;
   p.probs = plan->d_probs;
   p.items = plan->d_items;

@@ -212,8 +212,8 @@ def test_batch_stacks_shared_column_problems(dev):
     """16- and 32-row band and block-diagonal problems run stacked into 64-row
     blocks over the union of their rows' columns; random ones and 64-row ones
     run as they are. Every product matches FP64 over two runs, and after new
-    values are written into the stacked problems' A (the copy into the stacked
-    blocks is refreshed by every run)."""
+    values are written into the stacked problems' A (every run reads the
+    member blocks from A's own values)."""
     specs = [
         (1024, 1024, 16, m.PATTERN_BAND, 0.1, 6.0, 256),       # stacks
         (1024, 1024, 32, m.PATTERN_BLOCKDIAG, 0.0, 128.0, 128),  # stacks
