@@ -24,11 +24,14 @@
 // columns (band and block-diagonal structures), the plan stacks them: the
 // union of their columns becomes one 64-row BCSR row whose blocks hold the
 // member rows' blocks and zeros, so one UMMA and one B panel serve 4 (or 2)
-// blocks. A run copies the current values into the stacked blocks (one small
-// kernel) and runs the 64-row pipeline. The plan stacks only when the union
-// saves at least 40 % of the panels and N is above 512 (at N = 256 the copy
-// launch measured 6-19 % slower than running the blocks as they are; at 1024
-// and 4096 stacking was 1.05-1.7x faster).
+// blocks. A run is one launch of the 64-row pipeline whose B-panel issuers
+// also copy each stacked block's member blocks from A's own values into the
+// stage (a member row with no block reads a box past the end of A: zeros), so
+// every run takes the current values. The plan stacks only when the union
+// saves at least 40 % of the panels and N is above 512 (measured when a copy
+// kernel built the stacked blocks before each run: at N = 256 that launch
+// made it 6-19 % slower than running the blocks as they are; at 1024 and 4096
+// stacking was 1.05-1.7x faster).
 //
 // The plan holds only what row_ptr (and, for a stacked plan, col_idx)
 // determines: any A with the same M, K, block shape, dtype and structure
@@ -57,7 +60,6 @@ struct spmm_bcsr_plan {
   int* s_row_ptr = nullptr;       // M/64 + 1
   int* s_col_idx = nullptr;       // stacked_blocks
   int* s_map = nullptr;           // stacked_blocks x stack: source block of each member row, or -1
-  void* s_vals = nullptr;         // stacked_blocks x 64 x 16 values, refilled by every run
 };
 
 namespace spmm {
@@ -68,19 +70,6 @@ constexpr int kSplitFactor = 3;     // split rows longer than 3x the average loa
 constexpr int kMaxParts = 64;
 constexpr int kStackKeepPct = 60;   // stack when the union has at most 60 % of the blocks
 constexpr int kStackMinN = 512;     // and N is larger: below, the copy launch costs more than it saves
-
-// One thread per 16-byte chunk of a member block in the stacked layout: chunk
-// x of member i (= stacked block * stack + member row) is chunk x of source
-// block map[i], or zeros.
-__global__ void k_stack_repack(const int4* __restrict__ src, const int* __restrict__ map, long long members,
-                               int chunks, int4* __restrict__ dst) {
-  const long long n = members * chunks;
-  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
-    const long long i = x / chunks;
-    const int b = __ldg(map + i);
-    dst[x] = b >= 0 ? __ldg(src + (long long)b * chunks + (x - i * chunks)) : make_int4(0, 0, 0, 0);
-  }
-}
 
 // The stacked structure of 16- or 32-row blocks: for each group of `st` block
 // rows (64 rows of C), the sorted union of their block columns, and per union
@@ -182,7 +171,6 @@ void plan_free(spmm_bcsr_plan* p) {
   cudaFree(p->s_row_ptr);
   cudaFree(p->s_col_idx);
   cudaFree(p->s_map);
-  cudaFree(p->s_vals);
   delete p;
 }
 
@@ -274,13 +262,12 @@ extern "C" spmm_status spmm_bcsr_plan_create(const spmm_bcsr_desc* A, int N, con
   }
   p->queue = p->counters + 2 * std::max(pairs, 1);
   if (st > 1) {
-    // the stacked structure, and room for the stacked values every run refills
+    // the stacked structure: row pointers, column indices and member map
     p->stack = st;
     p->stacked_blocks = (long long)sci.size();
     if (cudaMalloc(&p->s_row_ptr, sizeof(int) * srp.size()) != cudaSuccess ||
         cudaMalloc(&p->s_col_idx, sizeof(int) * sci.size()) != cudaSuccess ||
-        cudaMalloc(&p->s_map, sizeof(int) * smap.size()) != cudaSuccess ||
-        cudaMalloc(&p->s_vals, (size_t)p->stacked_blocks * 64 * 16 * 2) != cudaSuccess) {
+        cudaMalloc(&p->s_map, sizeof(int) * smap.size()) != cudaSuccess) {
       plan_free(p);
       return fail(SPMM_ERR_CUDA, "stacked plan allocation failed");
     }
@@ -332,20 +319,13 @@ extern "C" spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* p, const spmm
   spmm_bcsr_desc a64;
   const spmm_bcsr_desc* Arun = A;
   if (p->stack > 1) {
-    // this run's values into the stacked 64-row blocks; the pipeline then
-    // reads them, so it waits for this kernel (no early start)
+    // the 64-row pipeline over the stacked structure; its stacked blocks are
+    // assembled in the stage from this A's member blocks
     if (!A->vals) return fail(SPMM_ERR_INVALID_ARG, "null values");
-    const int chunks = p->bR * 2;   // 16-byte chunks of a bR x 16 block of 2-byte values
-    const long long n = p->stacked_blocks * p->stack * chunks;
-    const long long grid = std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
-    k_stack_repack<<<(unsigned)grid, 256, 0, s>>>(static_cast<const int4*>(A->vals), p->s_map,
-                                                  p->stacked_blocks * p->stack, chunks, static_cast<int4*>(p->s_vals));
-    SPMM_CUDA_TRY(cudaGetLastError());
     a64 = *A;
     a64.bR = 64;
     a64.row_ptr = p->s_row_ptr;
     a64.col_idx = p->s_col_idx;
-    a64.vals = p->s_vals;
     a64.vals_lo = nullptr;
     a64.scales = nullptr;
     Arun = &a64;
@@ -364,7 +344,12 @@ extern "C" spmm_status spmm_bcsr_plan_run_ex(const spmm_bcsr_plan* p, const spmm
   r.counters = p->counters;
   r.plan_items = p->n_items;
   r.queue = p->queue;
-  r.inputs_ready = (flags & SPMM_RUN_INPUTS_READY) != 0 && p->stack == 1;
+  r.inputs_ready = (flags & SPMM_RUN_INPUTS_READY) != 0;
+  if (p->stack > 1) {
+    r.stack_map = p->s_map;
+    r.stack = p->stack;
+    r.member_bR = p->bR;
+  }
   return launch_tc(r);
 }
 

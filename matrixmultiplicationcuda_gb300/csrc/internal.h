@@ -95,6 +95,12 @@ struct LaunchRequest {
   // writes A or B: the pipeline's copies and MMAs may start before the
   // previous kernel has finished (plans only)
   bool inputs_ready = false;
+  // stacked plan: A describes the 64-row stacked structure over the values of
+  // the original member_bR-row blocks; each stacked block is `stack` members,
+  // stack_map[block * stack + t] = member t's source block, or -1 (zeros)
+  const int* stack_map = nullptr;
+  int stack = 1;
+  int member_bR = 0;
 };
 // The tcgen05 pipeline's column tile and CTAs per SM for a product (false when
 // it has no kernel for it): what a plan builds its item list for.

@@ -36,6 +36,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include "csr.cuh"
 #include "internal.h"
 #include "ptx.cuh"
@@ -86,6 +87,12 @@ struct TcParams {
   // is its exponent) and B's scale (applied in the epilogue)
   const float* scales;
   float b_scale;
+  // stacked plan (stk > 1, fp16 / bf16, 64-row kernels): each 64-row block is
+  // assembled in the stage from stk member blocks of mbR rows of A's own
+  // values; smap holds, per stacked block and member, the source block or -1
+  // (rows of zeros, read from row oob_row, past the end of A's tensor map)
+  const int* smap;
+  int stk, mbR, oob_row;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* ptr) {
@@ -128,6 +135,8 @@ template <int BR, int NT, int STAGES, int MODE, int ACC, int G>
 struct TcCfg {
   static constexpr bool kSplit = MODE == MODE_SPLIT;
   static constexpr bool kE4 = MODE == MODE_E4M3;
+  // a stacked plan's 64-row blocks are assembled from member blocks (fp16 / bf16)
+  static constexpr bool kStackable = (MODE == MODE_F16 || MODE == MODE_BF16) && BR == 64;
   static constexpr int kParts = kSplit ? 2 : 1;
   static constexpr int kJ = NT / 128;                 // 128-column MMA slices per item
   // UMMA issuing threads: one thread's issue rate bounds the pipeline (a UMMA
@@ -387,7 +396,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           // takes its later groups' DRAM latency off their copies (measured
           // 1-2 % on back-to-back plans of the headline product; no effect on
           // e4m3 or on a launch timed alone)
-          if (end > start) tma_prefetch_l2(p.avals + (size_t)start * Cfg::kABytes, (uint32_t)((end - start) * Cfg::kABytes));
+          if (end > start && p.stk <= 1)
+            tma_prefetch_l2(p.avals + (size_t)start * Cfg::kABytes, (uint32_t)((end - start) * Cfg::kABytes));
         }
         int gi = 0;
         for (int j0 = start; j0 < end; j0 += G, ++gs, ++gi) {
@@ -422,6 +432,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             // memory and in the slot, one bulk copy
             tma_bulk_g2s(smem_u32(a_dst), p.avals + (size_t)j0 * Cfg::kABytes, (uint32_t)(n * Cfg::kABytes), fb,
                          pol_a);
+          } else if (Cfg::kStackable && p.stk > 1) {
+            // a stacked block's members are copied by the B issuers
           } else if (n == G) {
             tma_tile_2d_g2s(smem_u32(a_dst), &tmAg, 0, y0, fb, pol_a);
             if (Cfg::kSplit) tma_tile_2d_g2s(smem_u32(a_dst + Cfg::kAPart), &tmAlog, 0, y0, fb, pol_a);
@@ -483,118 +495,161 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       end = __shfl_sync(0xffffffffu, end, 0);
       nt = __shfl_sync(0xffffffffu, nt, 0);
       if (!ok || item < 0) break;
-      int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
-      // e4m3, the scale writer (issuer 3): the blocks' scales, staged like the column indices
-      float mysc = 1.f;
-      if constexpr (Cfg::kE4) {
-        if (bidx == kScaleWriter) mysc = lane < end - start ? __ldg(p.scales + start + lane) : 1.f;
-      }
-      for (int base = start; base < end && !failed; base += 32) {
-        const int cnt = min(32, end - base);
-        const int cur = mycol;
-        const float cursc = mysc;
-        if (base + 32 < end) mycol = lane < end - base - 32 ? __ldg(p.col_idx + base + 32 + lane) : 0;
-        if constexpr (Cfg::kE4) {
-          if (bidx == kScaleWriter && base + 32 < end)
-            mysc = lane < end - base - 32 ? __ldg(p.scales + base + 32 + lane) : 1.f;
-        }
-        for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
-          const int n = min(G, cnt - i0);
-          const int s = (int)(gs % STAGES);
-          // Wait for the slot only in groups this issuer copies into: such a
-          // group cannot be released without its bytes, so the slot's empty
-          // barrier is at most one phase ahead. (An issuer that also waited in
-          // groups it has no block in could fall two phases behind and miss a
-          // parity flip.) Issuer 0 copies into every group, and so does the
-          // e4m3 scale writer (its arrival is part of every group's full barrier).
-          // The parity test is only valid when group gs - 2 * STAGES has been
-          // consumed (otherwise a stale parity reads as free). Consumption is in
-          // order, so the wait in an issuer's previous group covers it as long as
-          // that group is at most STAGES groups back: issuers skip only an item's
-          // last, partial group, and the lead publishes an item once the group
-          // 2 * STAGES before its first has been consumed (claim_ahead = STAGES - 1).
-          // (Rotating the block-to-issuer map over groups of fewer than four
-          // blocks breaks this and was measured to corrupt a slot.)
-          const bool writes = bidx < n || (Cfg::kE4 && bidx == kScaleWriter);
-          int bad = 0;
-          if (lane == 0 && writes && gs >= (uint32_t)STAGES &&
-              !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
-            atomicOr(p.err, 4u);
-            bad = 1;
-          }
-          failed = __shfl_sync(0xffffffffu, bad, 0);
-          if (failed) break;
-          uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
-          for (int b = bidx; b < n; b += kBIssuers) {
-            const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
-            if constexpr (!Cfg::kSplit && !Cfg::kE4) {
-              if (col < 0 && p.gather_rows) {
-                // Gather block: its panel is 16 arbitrary B rows. Lane L < 4 * (NT / 64)
-                // copies rows 4q .. 4q + 3 (q = L % 4) of 64-column box L / 4 with one
-                // tile::gather4 (tmBlo is then the one-row-box view of B), into the
-                // box's rows 4q .. 4q + 3: the image of a 16-row box copy. Padding
-                // rows index K, past the end of B, and read zeros.
-                const long long g = -(long long)col - 1;
-                const int kk = lane < 16 ? __ldg(p.gather_rows + 16 * g + lane) : 0;
-                const int q = lane & 3;
-                const int y0 = __shfl_sync(0xffffffffu, kk, 4 * q);
-                const int y1 = __shfl_sync(0xffffffffu, kk, 4 * q + 1);
-                const int y2 = __shfl_sync(0xffffffffu, kk, 4 * q + 2);
-                const int y3 = __shfl_sync(0xffffffffu, kk, 4 * q + 3);
-                if (lane < 4 * (NT / 64)) {
-                  const int bx = lane >> 2;
-                  tma_gather4_g2s(smem_u32(b_dst0 + (size_t)b * Cfg::kPanelBytes + bx * Cfg::kBoxBytes + q * 512),
-                                  &tmBlo, nt * NT + bx * 64, y0, y1, y2, y3, full0 + 8 * s, pol_b);
-                }
-                continue;
-              }
-            }
-            if (lane == 0) {
-              const uint32_t fb = full0 + 8 * s;
-              // e4m3: a partial group's panels take the slot's last slots
-              const int slot = Cfg::kE4 ? G - n + b : b;
-              uint8_t* b_dst = b_dst0 + (size_t)slot * Cfg::kPanelBytes * Cfg::kParts;
-              const int y = col * 16;
-              if (p.panel3d) {
-                tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, y, nt * (NT / Cfg::kBoxCols), fb, pol_b);
-                if (Cfg::kSplit)
-                  tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, y, nt * (NT / 64), fb, pol_b);
-              } else {
+      // One pass over the item's blocks. A stacked plan also copies, per
+      // stacked block, its member blocks from A's values into the block's A
+      // slot; the two cases are separate instantiations, so the plain path
+      // carries none of the member work.
+      auto issue_item = [&](auto stacked_tag) {
+        constexpr bool kStacked = decltype(stacked_tag)::value;
+        // member blocks take the lead's policy for A
+        const uint64_t pol_a = kStacked ? l2_policy_evict_first() : 0ull;
+        int mycol = lane < end - start ? __ldg(p.col_idx + start + lane) : 0;
+        // a stacked plan: each lane also stages the member source blocks of its
+        // stacked block (stk of them, -1 where the member row has no block)
+        const int stk = kStacked ? p.stk : 1;
+        auto load_members = [&](int j, int (&mm)[4]) {
 #pragma unroll
-                for (int bx = 0; bx < NT / Cfg::kBoxCols; ++bx) {
-                  tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), &tmB, nt * NT + bx * Cfg::kBoxCols, y, fb,
-                                  pol_b);
+          for (int t = 0; t < 4; ++t) mm[t] = (t < stk && j < end) ? __ldg(p.smap + (long long)j * stk + t) : -1;
+        };
+        int mym[4] = {-1, -1, -1, -1};
+        if constexpr (kStacked) load_members(start + lane, mym);
+        // e4m3, the scale writer (issuer 3): the blocks' scales, staged like the column indices
+        float mysc = 1.f;
+        if constexpr (Cfg::kE4) {
+          if (bidx == kScaleWriter) mysc = lane < end - start ? __ldg(p.scales + start + lane) : 1.f;
+        }
+        for (int base = start; base < end && !failed; base += 32) {
+          const int cnt = min(32, end - base);
+          const int cur = mycol;
+          [[maybe_unused]] const float cursc = mysc;
+          int curm[4] = {mym[0], mym[1], mym[2], mym[3]};
+          if constexpr (kStacked)
+            if (base + 32 < end) load_members(base + 32 + lane, mym);
+          if (base + 32 < end) mycol = lane < end - base - 32 ? __ldg(p.col_idx + base + 32 + lane) : 0;
+          if constexpr (Cfg::kE4) {
+            if (bidx == kScaleWriter && base + 32 < end)
+              mysc = lane < end - base - 32 ? __ldg(p.scales + base + 32 + lane) : 1.f;
+          }
+          for (int i0 = 0; i0 < cnt; i0 += G, ++gs) {
+            const int n = min(G, cnt - i0);
+            const int s = (int)(gs % STAGES);
+            // Wait for the slot only in groups this issuer copies into: such a
+            // group cannot be released without its bytes, so the slot's empty
+            // barrier is at most one phase ahead. (An issuer that also waited in
+            // groups it has no block in could fall two phases behind and miss a
+            // parity flip.) Issuer 0 copies into every group, and so does the
+            // e4m3 scale writer (its arrival is part of every group's full barrier).
+            // The parity test is only valid when group gs - 2 * STAGES has been
+            // consumed (otherwise a stale parity reads as free). Consumption is in
+            // order, so the wait in an issuer's previous group covers it as long as
+            // that group is at most STAGES groups back: issuers skip only an item's
+            // last, partial group, and the lead publishes an item once the group
+            // 2 * STAGES before its first has been consumed (claim_ahead = STAGES - 1).
+            // (Rotating the block-to-issuer map over groups of fewer than four
+            // blocks breaks this and was measured to corrupt a slot.)
+            const bool writes = bidx < n || (Cfg::kE4 && bidx == kScaleWriter);
+            int bad = 0;
+            if (lane == 0 && writes && gs >= (uint32_t)STAGES &&
+                !mbar_wait(empty0 + 8 * s, ((gs / STAGES) + 1) & 1, p.timeout_ns)) {
+              atomicOr(p.err, 4u);
+              bad = 1;
+            }
+            failed = __shfl_sync(0xffffffffu, bad, 0);
+            if (failed) break;
+            uint8_t* b_dst0 = smem + (size_t)s * Cfg::kStage + Cfg::kAStage;
+            for (int b = bidx; b < n; b += kBIssuers) {
+              const int col = __shfl_sync(0xffffffffu, cur, i0 + b);
+              int src[4] = {-1, -1, -1, -1};
+              if constexpr (kStacked) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) src[t] = __shfl_sync(0xffffffffu, curm[t], i0 + b);
+              }
+              if constexpr (!Cfg::kSplit && !Cfg::kE4 && !kStacked) {
+                if (col < 0 && p.gather_rows) {
+                  // Gather block: its panel is 16 arbitrary B rows. Lane L < 4 * (NT / 64)
+                  // copies rows 4q .. 4q + 3 (q = L % 4) of 64-column box L / 4 with one
+                  // tile::gather4 (tmBlo is then the one-row-box view of B), into the
+                  // box's rows 4q .. 4q + 3: the image of a 16-row box copy. Padding
+                  // rows index K, past the end of B, and read zeros.
+                  const long long g = -(long long)col - 1;
+                  const int kk = lane < 16 ? __ldg(p.gather_rows + 16 * g + lane) : 0;
+                  const int q = lane & 3;
+                  const int y0 = __shfl_sync(0xffffffffu, kk, 4 * q);
+                  const int y1 = __shfl_sync(0xffffffffu, kk, 4 * q + 1);
+                  const int y2 = __shfl_sync(0xffffffffu, kk, 4 * q + 2);
+                  const int y3 = __shfl_sync(0xffffffffu, kk, 4 * q + 3);
+                  if (lane < 4 * (NT / 64)) {
+                    const int bx = lane >> 2;
+                    tma_gather4_g2s(smem_u32(b_dst0 + (size_t)b * Cfg::kPanelBytes + bx * Cfg::kBoxBytes + q * 512),
+                                    &tmBlo, nt * NT + bx * 64, y0, y1, y2, y3, full0 + 8 * s, pol_b);
+                  }
+                  continue;
+                }
+              }
+              if (lane == 0) {
+                const uint32_t fb = full0 + 8 * s;
+                if constexpr (kStacked) {
+                  // the stacked 64-row block: member t's rows at t * mbR, from
+                  // its source block, or a box past the end of A (zeros)
+                  uint8_t* a_dst = smem + (size_t)s * Cfg::kStage + (size_t)b * Cfg::kABytes;
+#pragma unroll
+                  for (int t = 0; t < 4; ++t)
+                    if (t < stk)
+                      tma_tile_2d_g2s(smem_u32(a_dst + t * p.mbR * 32), &tmA1, 0,
+                                      src[t] >= 0 ? src[t] * p.mbR : p.oob_row, fb, pol_a);
+                }
+                // e4m3: a partial group's panels take the slot's last slots
+                const int slot = Cfg::kE4 ? G - n + b : b;
+                uint8_t* b_dst = b_dst0 + (size_t)slot * Cfg::kPanelBytes * Cfg::kParts;
+                const int y = col * 16;
+                if (p.panel3d) {
+                  tma_tile_3d_g2s(smem_u32(b_dst), &tmB, 0, y, nt * (NT / Cfg::kBoxCols), fb, pol_b);
                   if (Cfg::kSplit)
-                    tma_tile_2d_g2s(smem_u32(b_dst + Cfg::kPanelBytes + bx * Cfg::kBoxBytes), &tmBlo,
-                                    nt * NT + bx * 64, y, fb, pol_b);
+                    tma_tile_3d_g2s(smem_u32(b_dst + Cfg::kPanelBytes), &tmBlo, 0, y, nt * (NT / 64), fb, pol_b);
+                } else {
+#pragma unroll
+                  for (int bx = 0; bx < NT / Cfg::kBoxCols; ++bx) {
+                    tma_tile_2d_g2s(smem_u32(b_dst + bx * Cfg::kBoxBytes), &tmB, nt * NT + bx * Cfg::kBoxCols, y, fb,
+                                    pol_b);
+                    if (Cfg::kSplit)
+                      tma_tile_2d_g2s(smem_u32(b_dst + Cfg::kPanelBytes + bx * Cfg::kBoxBytes), &tmBlo,
+                                      nt * NT + bx * 64, y, fb, pol_b);
+                  }
                 }
               }
             }
-          }
-          if constexpr (Cfg::kE4) {
-            if (bidx == kScaleWriter) {
-              // After its own copies are in flight: the group's 512-byte scale
-              // tile, every 32-bit word holding byte b = block b's scale in
-              // UE8M0, the exponent field of a power-of-two fp32 (bit 64 of
-              // the error word flags a scale that is not one); then the proxy
-              // fence that makes it visible to tcgen05.cp, and the arrival the
-              // group's full barrier waits for.
-              uint32_t w = 0;
-              for (int b = 0; b < n; ++b) {
-                const uint32_t bits = __float_as_uint(__shfl_sync(0xffffffffu, cursc, i0 + b));
-                const uint32_t e = (bits >> 23) & 0xFFu;
-                if (lane == 0 && ((bits & 0x807FFFFFu) != 0u || e == 0u || e == 0xFFu)) atomicOr(p.err, 64u);
-                w |= e << (8 * b);
+            if constexpr (Cfg::kE4) {
+              if (bidx == kScaleWriter) {
+                // After its own copies are in flight: the group's 512-byte scale
+                // tile, every 32-bit word holding byte b = block b's scale in
+                // UE8M0, the exponent field of a power-of-two fp32 (bit 64 of
+                // the error word flags a scale that is not one); then the proxy
+                // fence that makes it visible to tcgen05.cp, and the arrival the
+                // group's full barrier waits for.
+                uint32_t w = 0;
+                for (int b = 0; b < n; ++b) {
+                  const uint32_t bits = __float_as_uint(__shfl_sync(0xffffffffu, cursc, i0 + b));
+                  const uint32_t e = (bits >> 23) & 0xFFu;
+                  if (lane == 0 && ((bits & 0x807FFFFFu) != 0u || e == 0u || e == 0xFFu)) atomicOr(p.err, 64u);
+                  w |= e << (8 * b);
+                }
+                *reinterpret_cast<uint4*>(smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff + 16 * lane) =
+                    make_uint4(w, w, w, w);
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(full0 + 8 * s);
               }
-              *reinterpret_cast<uint4*>(smem + (size_t)s * Cfg::kStage + Cfg::kScaleOff + 16 * lane) =
-                  make_uint4(w, w, w, w);
-              fence_proxy_async_smem();
-              __syncwarp();
-              if (lane == 0) mbar_arrive(full0 + 8 * s);
             }
           }
         }
+      };
+      if constexpr (Cfg::kStackable) {
+        if (p.stk > 1) {
+          issue_item(std::true_type{});
+          continue;
+        }
       }
+      issue_item(std::false_type{});
     }
   } else if (warp == 1 || (Cfg::kIssuers == 2 && warp == 10)) {
     // ------------------------------ MMA issuers ----------------------------------
@@ -930,7 +985,13 @@ spmm_status launch_tc(const LaunchRequest& r) {
       std::max<unsigned long long>((unsigned long long)(A.M / A.bR) * (A.K / 16) * A.bR, 256ull);
   if (r.gather_rows)   // gather blocks come on top of at most K / 16 stored blocks per row
     rows_bound = std::max<unsigned long long>(rows_bound, (unsigned long long)r.total_blocks * A.bR);
-  if (rows_bound >= (1ull << 31)) return fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline");
+  const bool stacked = r.stack > 1;
+  // (a stacked run also names row rows_bound, the first past the end, as the source of its zero members)
+  if (rows_bound >= (1ull << 31) - (stacked ? 64 : 0))
+    return fail(SPMM_ERR_UNSUPPORTED, "A too large for the tcgen05 pipeline");
+  if (stacked && (A.bR != 64 || (mode != MODE_F16 && mode != MODE_BF16) || r.csr || r.gather_rows || !r.stack_map ||
+                  (r.member_bR != 16 && r.member_bR != 32) || r.stack * r.member_bR != 64))
+    return fail(SPMM_ERR_UNSUPPORTED, "a stacked run takes 16- or 32-row fp16 / bf16 blocks on the 64-row pipeline");
   CUtensorMap tmA1, tmAg, tmAlo1, tmAlog, tmB, tmBlo;
   const void* vals = A.vals ? A.vals : B.data;   // no stored blocks: never dereferenced
   // A's values as a [rows x 16] matrix: 16-bit with 32-byte swizzle (the UMMA
@@ -939,7 +1000,10 @@ spmm_status launch_tc(const LaunchRequest& r) {
   const CUtensorMapDataType adt = e4 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
   const CUtensorMapSwizzle aswz = e4 ? CU_TENSOR_MAP_SWIZZLE_NONE : CU_TENSOR_MAP_SWIZZLE_32B;
   const uint64_t arow = e4 ? 16 : 32;
-  spmm_status st = encode_tile_map_2d(&tmA1, adt, vals, 16, rows_bound, arow, 16, (uint32_t)A.bR, aswz);
+  // (a stacked run: A.vals holds the member blocks, bR = member_bR rows each,
+  // and the same rows bound: (M / bR) * (K / 16) * bR rows for any bR)
+  spmm_status st = encode_tile_map_2d(&tmA1, adt, vals, 16, rows_bound, arow, 16,
+                                      (uint32_t)(stacked ? r.member_bR : A.bR), aswz);
   if (st != SPMM_OK) return st;
   st = encode_tile_map_2d(&tmAg, adt, vals, 16, rows_bound, arow, 16, (uint32_t)(e->group * A.bR), aswz);
   if (st != SPMM_OK) return st;
@@ -1012,6 +1076,10 @@ spmm_status launch_tc(const LaunchRequest& r) {
   p.scales = A.scales;
   p.avals = static_cast<const uint8_t*>(A.vals);
   p.b_scale = e4 ? B.scale : 1.0f;
+  p.smap = stacked ? r.stack_map : nullptr;
+  p.stk = stacked ? r.stack : 1;
+  p.mbR = stacked ? r.member_bR : 0;
+  p.oob_row = (int)rows_bound;
   if (r.items) {
     if (p.split > 1 || r.csr || r.gather_rows || (p.queue && !r.queue))
       return fail(SPMM_ERR_UNSUPPORTED, "a planned product runs without split-K, CSR part or shared work queue");

@@ -364,7 +364,7 @@ def test_plan_stacks_short_blocks(dev, bR, pattern, param, N, cfg):
     assert torch.equal(C, ref)
     A2 = m.BCSR.from_host(M, K, bR, rp, ci, -2 * vals, m.DType.F16, device=dev)   # same structure
     torch.cuda.synchronize()
-    plan.run(A2, B, C=C, inputs_ready=True)   # a stacked plan runs without the early start
+    plan.run(A2, B, C=C, inputs_ready=True)   # the early start reads the new values too
     m.device_error_check()
     assert torch.equal(C, -2 * ref)
     plan.close()
@@ -385,8 +385,8 @@ def test_plan_does_not_stack(dev, M, pattern, density, N):
 
 
 def test_plan_stacked_bf16_in_cuda_graph(dev):
-    """A stacked run is two launches (the copy into 64-row blocks, then the
-    pipeline); captured in a graph and replayed it matches the eager product."""
+    """A stacked run (one launch that assembles the 64-row blocks from A's own
+    values) captured in a graph and replayed matches the eager product."""
     M = K = 8192
     N = 1024
     rp, ci, vals, A = _int_bcsr(M, K, 16, m.PATTERN_BAND, 0.2, 8, 15, dev, m.DType.BF16)
@@ -411,3 +411,43 @@ def test_plan_stacked_bf16_in_cuda_graph(dev):
         m.device_error_check()
         assert torch.equal(C, eager)
     plan.close()
+
+
+@pytest.mark.parametrize("bR,dtype,N", [(16, m.DType.F16, 1024), (32, m.DType.BF16, 1000), (16, m.DType.BF16, 776)])
+def test_plan_stacked_every_entry_inputs_ready_chain(dev, bR, dtype, N):
+    """Every plan entry of the tuner table that stacks this product (band
+    rows sharing their columns): the stacked run equals the unplanned product
+    exactly, and so do twelve launches chained with SPMM_RUN_INPUTS_READY
+    round-robin over three B (integer inputs). N = 1000 and 776 take the
+    2-D panel path."""
+    from matrixmultiplicationcuda_gb300 import tuner
+    M, K = 2048, 3072
+    rp, ci, vals, A = _int_bcsr(M, K, bR, m.PATTERN_BAND, 0.2, 8, 21 + bR, dev, dtype)
+    tdt = torch.float16 if dtype == m.DType.F16 else torch.bfloat16
+    B0 = torch.from_numpy(np.random.default_rng(22).integers(-2, 3, (K, N)).astype(np.float32)).to(dev).to(tdt)
+    Bs = [B0] + [(B0 * (s + 2)).contiguous() for s in range(2)]
+    refs = [m.spmm(A, B, N=N) for B in Bs]
+    stacked = 0
+    for cfg in [c for c in tuner.configs() if tuner.is_plan(c)]:
+        try:
+            plan = m.BcsrPlan(A, N, cfg)
+        except m.SpmmError:
+            continue   # no 64-row kernel for this entry's tile at this N, and none at bR either
+        if plan.stacking()[0] == 1:
+            plan.close()
+            continue
+        stacked += 1
+        C0 = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+        plan.run(A, Bs[0], C=C0)
+        m.device_error_check()
+        assert torch.equal(C0, refs[0]), tuner.config_name(cfg)
+        Cs = [torch.full((M, N), float("nan"), dtype=torch.float32, device=dev) for _ in Bs]
+        torch.cuda.synchronize()
+        for i in range(12):
+            plan.run(A, Bs[i % 3], C=Cs[i % 3], inputs_ready=True)
+        torch.cuda.synchronize()
+        m.device_error_check()
+        for C, ref in zip(Cs, refs):
+            assert torch.equal(C, ref), tuner.config_name(cfg)
+        plan.close()
+    assert stacked >= 3
