@@ -427,12 +427,12 @@ spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr
  *   block rows that make up 64 rows of C share most of their block columns
  *   (the union holds at most 60 % of their blocks, as in band and
  *   block-diagonal structures), the plan stacks them into 64-row blocks with
- *   zeros where a row has no block, and a run first copies A's values into
- *   them (one small kernel) and then runs the 64-row pipeline: one UMMA and
- *   one B panel for up to 4 blocks. A stacked plan is built from col_idx as
- *   well, so A's column indices must stay the plan's; it runs without the
- *   early start of SPMM_RUN_INPUTS_READY (its pipeline reads the copy made
- *   just before).
+ *   zeros where a row has no block, and a run is one launch of the 64-row
+ *   pipeline that assembles each stacked block in shared memory from A's own
+ *   blocks: one UMMA and one B panel for up to 4 blocks. A stacked plan is
+ *   built from col_idx as well, so A's column indices must stay the plan's;
+ *   its values may change, and it takes the early start of
+ *   SPMM_RUN_INPUTS_READY like any plan.
  * spmm_bcsr_plan_info: item count, split rows (row and column-tile pairs),
  * and the configuration the plan runs (for a stacked plan, the 64-row one).
  * spmm_bcsr_plan_stacking: block rows per stacked row (1: not stacked) and
