@@ -69,7 +69,7 @@ constexpr int kMinPartBlocks = 8;   // shorter parts are not worth a hand-off
 constexpr int kSplitFactor = 3;     // split rows longer than 3x the average load per CTA slot
 constexpr int kMaxParts = 64;
 constexpr int kStackKeepPct = 60;   // stack when the union has at most 60 % of the blocks
-constexpr int kStackMinN = 512;     // and N is larger: below, the copy launch costs more than it saves
+constexpr int kStackMinN = 512;     // and N is larger (the threshold measured with a copy launch per run)
 
 // The stacked structure of 16- or 32-row blocks: for each group of `st` block
 // rows (64 rows of C), the sorted union of their block columns, and per union
