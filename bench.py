@@ -895,6 +895,10 @@ def run_profile_families(names, launches):
       plan      k_bcsr_tc on a per-matrix plan: A 8192^2, 64x16 blocks, log-normal
                 rows (5 %, CV 1.5), N 512, bf16, 256-column tile (rows far above
                 the average load split into parts)
+      plan_stack  k_bcsr_tc on a stacked per-matrix plan: A 8192^2, 16x16 blocks,
+                band (20 %, the union of each 64 rows' columns ~29 % of the
+                blocks), N 4096, fp16; four 16-row blocks assembled per 64-row
+                block in the stage
       dense     k_dense_tc: the native dense comparator, A 8192 x 8192, B 8192 x 1024, fp16
       plan_rot  the headline run: fp16 plan, 512-column tile, one accumulator,
                 launches chained inputs-ready over six rotating copies (five
@@ -1063,6 +1067,18 @@ def run_profile_families(names, launches):
         plan = m.BcsrPlan(A, 512, m.Config(kernel=2, n_tile=256, acc_buffers=2))
         run(lambda: plan.run(A, B, C=C))
         print("plan: (items, split rows) =", plan.info()[:2])
+        plan.close()
+    if "plan_stack" in only:
+        M = K = 8192
+        N = 4096
+        rp, ci = m.gen_structure(M, K, 16, m.PATTERN_BAND, 0.2, 8, seed=3)
+        vals = m.gen_values(len(ci), 16, 16, m.DIST_UNIFORM, seed=4)
+        A = m.BCSR.from_host(M, K, 16, rp, ci, vals, m.DType.F16, device=dev)
+        B = torch.from_numpy(m.gen_dense(K, N, m.DIST_UNIFORM, seed=5)).to(dev).half()
+        C = torch.empty((M, N), dtype=torch.float32, device=dev)
+        plan = m.BcsrPlan(A, N)
+        run(lambda: plan.run(A, B, C=C))
+        print("plan_stack: nnzb=%d, (rows per stack, stacked blocks) =" % len(ci), plan.stacking())
         plan.close()
     if "dense" in only:
         g = torch.Generator().manual_seed(0)
