@@ -167,3 +167,29 @@ def test_stack_structure_rejects():
         m.stack_structure(np.array([0, 2, 2, 2, 2], np.int32), np.array([3, 3], np.int32), 4)   # repeated column
     with pytest.raises(m.SpmmError):
         m.stack_structure(np.array([0, 1, 2, 3], np.int32), np.array([0, 1, 2], np.int32), 2)   # 3 rows, stacks of 2
+
+
+@pytest.mark.parametrize("bR", [16, 32])
+def test_stacked_blocks_give_the_same_product(bR):
+    """The 64-row blocks a stacked run multiplies: stacked block j holds member
+    t's bR rows at rows t * bR .. (t + 1) * bR - 1 (source block map[j, t], or
+    zeros for -1), the layout the pipeline assembles in its stage. Their 64-row
+    product is the original one (FP64 oracle; zero blocks add exact zeros and
+    each row keeps its column order)."""
+    from oracle import oracle
+    M = K = 1024
+    rp, ci = m.gen_structure(M, K, bR, m.PATTERN_BAND, 0.2, 4, seed=31)
+    st = 64 // bR
+    srp, sci, smap = m.stack_structure(rp, ci, st)
+    rng = np.random.default_rng(32)
+    vals = rng.standard_normal(len(ci) * bR * 16)
+    blocks = vals.reshape(-1, bR, 16)
+    stacked = np.zeros((len(sci), 64, 16))
+    for j in range(len(sci)):
+        for t in range(st):
+            if smap[j, t] >= 0:
+                stacked[j, t * bR:(t + 1) * bR] = blocks[smap[j, t]]
+    B = rng.standard_normal((K, 48))
+    ref = oracle.bcsr_matmul_f64(rp, ci, vals, bR, 16, B)
+    got = oracle.bcsr_matmul_f64(srp, sci, stacked.reshape(-1), 64, 16, B)
+    assert np.array_equal(got, ref)
