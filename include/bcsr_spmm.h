@@ -423,7 +423,7 @@ spmm_status spmm_cost_model_select(const spmm_cost_model* model, const spmm_bcsr
  * at a time (its queue and counters are its own; use one plan per stream for
  * concurrent launches). cfg: kernel 0 or 2, no split-K, schedule 0 or 1
  * (either way the plan's own queue; _info reports schedule 1).
- * 16- and 32-row blocks (fp16 / bf16, M a multiple of 64, N > 512): when the 4 (or 2)
+ * 16- and 32-row blocks (fp16 / bf16, M a multiple of 64, N > 256): when the 4 (or 2)
  *   block rows that make up 64 rows of C share most of their block columns
  *   (the union holds at most 60 % of their blocks, as in band and
  *   block-diagonal structures), the plan stacks them into 64-row blocks with

@@ -28,10 +28,12 @@
 // also copy each stacked block's member blocks from A's own values into the
 // stage (a member row with no block reads a box past the end of A: zeros), so
 // every run takes the current values. The plan stacks only when the union
-// saves at least 40 % of the panels and N is above 512 (measured when a copy
-// kernel built the stacked blocks before each run: at N = 256 that launch
-// made it 6-19 % slower than running the blocks as they are; at 1024 and 4096
-// stacking was 1.05-1.7x faster).
+// saves at least 40 % of the panels and N is above 256. Measured on 8192^2
+// band and block-diagonal products at 20 %: at N = 512 stacking ran 1.0-1.24x
+// faster as one cold launch and 1.07-1.46x back to back; at N = 256 it ran
+// 0.87-1.0x cold, 16-row products 1.23-1.25x back to back and 32-row ones
+// 0.93-0.95x. (A version that built the stacked blocks with a copy kernel
+// before each run needed N above 512.)
 //
 // The plan holds only what row_ptr (and, for a stacked plan, col_idx)
 // determines: any A with the same M, K, block shape, dtype and structure
@@ -69,7 +71,7 @@ constexpr int kMinPartBlocks = 8;   // shorter parts are not worth a hand-off
 constexpr int kSplitFactor = 3;     // split rows longer than 3x the average load per CTA slot
 constexpr int kMaxParts = 64;
 constexpr int kStackKeepPct = 60;   // stack when the union has at most 60 % of the blocks
-constexpr int kStackMinN = 512;     // and N is larger (the threshold measured with a copy launch per run)
+constexpr int kStackMinN = 256;     // and N is larger
 
 // The stacked structure of 16- or 32-row blocks: for each group of `st` block
 // rows (64 rows of C), the sorted union of their block columns, and per union

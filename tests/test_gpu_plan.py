@@ -372,7 +372,7 @@ def test_plan_stacks_short_blocks(dev, bR, pattern, param, N, cfg):
 
 @pytest.mark.parametrize("M,pattern,density,N", [(4096, m.PATTERN_RANDOM, 0.05, 1024),     # columns rarely shared
                                                  (4096 + 16, m.PATTERN_BAND, 0.2, 1024),  # M not a multiple of 64
-                                                 (4096, m.PATTERN_BAND, 0.2, 512)])       # N too small to pay
+                                                 (4096, m.PATTERN_BAND, 0.2, 256)])       # N too small to pay
 def test_plan_does_not_stack(dev, M, pattern, density, N):
     K = 4096
     rp, ci, vals, A = _int_bcsr(M, K, 16, pattern, density, 8, 13, dev)
