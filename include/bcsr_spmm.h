@@ -263,6 +263,10 @@ typedef struct spmm_problem {
   int ldc;
 } spmm_problem;
 typedef struct spmm_batch_plan spmm_batch_plan;
+/* cfg (NULL: defaults): n_tile 0 (128 columns for N <= 128, else 256), 128 or
+ * 256; stages 0, 2, 4 or 8 (the ring in groups: two groups of four blocks by
+ * default, four groups of two when some problem runs stacked, eight of one);
+ * ctas_per_sm 0 (as many as fit, at most 2) or fewer. */
 spmm_status spmm_batch_plan_create(const spmm_problem* problems, int count,
                                    const spmm_config* cfg, spmm_batch_plan** plan_out);
 spmm_status spmm_batch_run(const spmm_batch_plan* plan, void* stream);
